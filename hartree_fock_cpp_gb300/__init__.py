@@ -1,0 +1,276 @@
+"""hartree_fock_cpp_gb300 -- GB300-native direct-SCF Fock-build engine behind
+the ERI/Fock call of KLYYCYNN/hartree_fock_cpp.
+
+Host-side mirror of the reference's interface for this path, over the C ABI
+of libhfx.so (include/hfx.h):
+
+  basis_construction(config, basis_set, param_path)   basis.hpp:157-262
+  schwarz_bounds(basis)                                integrals.hpp:732-752
+  ERI_GPU(basis, threshold)                            eri.cu:20-89 (packed eri_index layout)
+  FockBuilder(...).repulsion_matrix(P)                 linalg.hpp:100-129 (direct, no stored tensor)
+  FockBuilder(...).coulomb_exchange(Pa, Pb)            linalg.hpp:215-296
+  rhf_diis(config, basis_set, param_path, ...)          scf.hpp:205-419
+  uhf_diis(config, basis_set, param_path, spin_occ, ...) scf.hpp:423-682
+
+``config`` is the reference's list of (symbol, (x, y, z)) pairs in bohr.
+Errors raise HfxError carrying the engine's status code; the engine has no
+CPU fallback (eri_device "CPU" is the reference's own stored-tensor path and
+is not part of this library).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import BASIS_PATH, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError, check, lib, ptr
+
+__all__ = ["Basis", "basis_construction", "schwarz_bounds", "ERI_GPU", "FockBuilder", "rhf_diis", "uhf_diis",
+           "one_electron", "measure_peaks", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED", "BASIS_PATH",
+           "eri_index", "pair_index"]
+
+
+def pair_index(a, b):                     # indexing.hpp:33-40
+    if a < b:
+        a, b = b, a
+    return a * (a + 1) // 2 + b
+
+
+def eri_index(i, j, k, l):                # indexing.hpp:42-53
+    ij, kl = pair_index(i, j), pair_index(k, l)
+    if ij < kl:
+        ij, kl = kl, ij
+    return ij * (ij + 1) // 2 + kl
+
+
+class Basis:
+    """Flat basis-function list (the reference's std::vector<basis_function>)."""
+
+    def __init__(self, centres, lmn, prim_offset, alpha, coeff, norm):
+        self.centres = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1, 3)
+        self.lmn = np.ascontiguousarray(lmn, dtype=np.int32).reshape(-1, 3)
+        self.prim_offset = np.ascontiguousarray(prim_offset, dtype=np.int32)
+        self.alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+        self.coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+        self.norm = np.ascontiguousarray(norm, dtype=np.float64)
+        self.K = self.lmn.shape[0]
+        self.c = _lib.Functions(self.K, self.centres.ctypes.data, self.lmn.ctypes.data, self.prim_offset.ctypes.data,
+                                self.alpha.ctypes.data, self.coeff.ctypes.data, self.norm.ctypes.data)
+
+    def ref(self):
+        return ctypes.byref(self.c)
+
+    def __len__(self):
+        return self.K
+
+
+def basis_construction(config, basis_set, param_path=None):
+    """basis.hpp:157-262 -- atoms in order, CSV shells in order, Cartesian
+    components in angmom_partition order, cart_norm per component."""
+    m = _lib.MoleculeArgs(config, basis_set, param_path)
+    K, n = ctypes.c_int(), ctypes.c_int()
+    check(lib.hfx_build_functions(m.ref(), ctypes.byref(K), ctypes.byref(n), None, None, None, None, None, None))
+    K, n = K.value, n.value
+    c, lmn, off = np.zeros(3 * K), np.zeros(3 * K, np.int32), np.zeros(K + 1, np.int32)
+    a, co, no = np.zeros(n), np.zeros(n), np.zeros(n)
+    check(lib.hfx_build_functions(m.ref(), None, None, ptr(c), ptr(lmn), ptr(off), ptr(a), ptr(co), ptr(no)))
+    return Basis(c, lmn, off, a, co, no)
+
+
+def _options(screening_threshold=1e-8, precision=HFX_PREC_FP64, fp32_threshold=0.0, device=0):
+    o = _lib.Options()
+    o.screening_threshold = screening_threshold
+    o.precision = precision
+    o.fp32_threshold = fp32_threshold
+    o.device = device
+    return o
+
+
+class FockBuilder:
+    """One device-resident job (basis, pair data, Schwarz table, quartet work
+    lists) reused for every Fock build of an SCF."""
+
+    def __init__(self, basis=None, *, config=None, basis_set=None, param_path=None, screening_threshold=1e-8,
+                 precision=HFX_PREC_FP64, fp32_threshold=0.0, device=0):
+        self._opt = _options(screening_threshold, precision, fp32_threshold, device)
+        self._job = ctypes.c_void_p()
+        if basis is not None:
+            self._basis = basis
+            check(lib.hfx_create(basis.ref(), ctypes.byref(self._opt), ctypes.byref(self._job)))
+        else:
+            self._mol = _lib.MoleculeArgs(config, basis_set, param_path)
+            check(lib.hfx_create_molecule(self._mol.ref(), ctypes.byref(self._opt), ctypes.byref(self._job)))
+        k = ctypes.c_int()
+        check(lib.hfx_nbasis(self._job, ctypes.byref(k)))
+        self.K = k.value
+
+    def close(self):
+        if self._job:
+            check(lib.hfx_destroy(self._job))
+            self._job = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _mat(self, P):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        if P.shape != (self.K, self.K):
+            raise HfxError(1, "density must be %d x %d" % (self.K, self.K))
+        return P
+
+    def schwarz_bounds(self):
+        Q = np.zeros(self.K * (self.K + 1) // 2)
+        check(lib.hfx_schwarz(self._job, ptr(Q)))
+        return Q
+
+    def repulsion_matrix(self, P):
+        """G = J[P] - 1/2 K[P] (linalg.hpp:100-129)."""
+        P = self._mat(P)
+        G = np.zeros_like(P)
+        check(lib.hfx_fock_rhf(self._job, ptr(P), ptr(G)))
+        return G
+
+    def coulomb_exchange(self, Pa, Pb):
+        """(J[Pa+Pb], K[Pa], K[Pb]) (linalg.hpp:215-296)."""
+        Pa, Pb = self._mat(Pa), self._mat(Pb)
+        J, Ka, Kb = np.zeros_like(Pa), np.zeros_like(Pa), np.zeros_like(Pa)
+        check(lib.hfx_fock_uhf(self._job, ptr(Pa), ptr(Pb), ptr(J), ptr(Ka), ptr(Kb)))
+        return J, Ka, Kb
+
+    def repulsion_matrix_device(self, dP_ptr, dG_ptr):
+        """Device-pointer variant (pointers as ints, K*K doubles each)."""
+        check(lib.hfx_fock_rhf_device(self._job, ctypes.c_void_p(dP_ptr), ctypes.c_void_p(dG_ptr)))
+
+    def coulomb_exchange_device(self, dPa, dPb, dJ, dKa, dKb):
+        check(lib.hfx_fock_uhf_device(self._job, *[ctypes.c_void_p(x) for x in (dPa, dPb, dJ, dKa, dKb)]))
+
+    def eri_unique(self, threshold=1e-8):
+        npair = self.K * (self.K + 1) // 2
+        out = np.zeros(npair * (npair + 1) // 2)
+        check(lib.hfx_eri_unique(self._job, threshold, ptr(out)))
+        return out
+
+    def stats(self):
+        s = _lib.BuildStats()
+        check(lib.hfx_last_build_stats(self._job, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _lib.BuildStats._fields_ if k != "reserved"}
+
+
+def schwarz_bounds(basis):
+    """integrals.hpp:732-752 on the device."""
+    with FockBuilder(basis, screening_threshold=-1.0) as fb:
+        return fb.schwarz_bounds()
+
+
+def ERI_GPU(basis, threshold=1e-8):
+    """Literal replacement of ERI_GPU (eri.cu:20-89): all unique ERIs in
+    eri_index order, zero where Q_ij*Q_kl < threshold."""
+    npair = basis.K * (basis.K + 1) // 2
+    out = np.zeros(npair * (npair + 1) // 2)
+    check(lib.hfx_eri_gpu(basis.ref(), threshold, ptr(out)))
+    return out
+
+
+def _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
+                 fp32_threshold):
+    o = _lib.ScfOptions()
+    o.max_iterations = max_it
+    o.epsilon = epsilon
+    o.damping = damping
+    o.screening_threshold = screening_threshold
+    o.energy_threshold = energy_threshold
+    o.charge = charge
+    o.precision = precision
+    o.fp32_threshold = fp32_threshold
+    return o
+
+
+def _check_device(eri_device):
+    if eri_device not in ("CPU", "GPU"):
+        raise HfxError(1, "unsupported ERI computing platform")      # scf.hpp:223-225
+    if eri_device == "CPU":
+        raise HfxError(5, "eri_device 'CPU' is the reference's stored-tensor path; this engine is the GPU path")
+
+
+def rhf_diis(config, basis_set, param_path=None, charge=0, eri_device="GPU", set_initial_density=False, P0=None,
+             max_it=10000, epsilon=1e-6, damping=0.3, screening_threshold=1e-8, energy_threshold=0.0,
+             precision=HFX_PREC_FP64, fp32_threshold=0.0, raise_on_nonconvergence=False):
+    """scf.hpp:205-419 with the direct GPU Fock build.  Returns a dict shaped
+    like the reference's rhf_data (types.hpp:50-73)."""
+    _check_device(eri_device)
+    m = _lib.MoleculeArgs(config, basis_set, param_path)
+    o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
+                     fp32_threshold)
+    K = ctypes.c_int()
+    check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
+    K = K.value
+    P0a = None
+    if set_initial_density:
+        P0a = np.ascontiguousarray(P0, dtype=np.float64).reshape(-1)
+        if P0a.size != K * K:
+            raise HfxError(1, "initial density matrix dimension inconsistent with basis size")
+    r = _lib.ScfResult()
+    dens, coef, mo = np.zeros((K, K)), np.zeros((K, K)), np.zeros(K)
+    st = lib.hfx_rhf_diis(m.ref(), ctypes.byref(o), ptr(P0a), ctypes.byref(r), ptr(dens), ptr(coef), ptr(mo))
+    if st != 0 and not (st == 6 and not raise_on_nonconvergence):
+        check(st)
+    return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
+                K=r.K, Ne=r.n_electrons, density=dens, coefficient=coef, mo_energy=mo, duration=r.seconds,
+                fock_ms=r.fock_ms, fock_builds=r.fock_builds, hardware=eri_device, BasisSet=basis_set,
+                charge=charge)
+
+
+def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_device="GPU",
+             set_initial_density=False, Pa0=None, Pb0=None, max_it=10000, epsilon=1e-6, damping=0.3,
+             screening_threshold=1e-8, energy_threshold=0.0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
+             raise_on_nonconvergence=False):
+    """scf.hpp:423-682 with the direct GPU J/Ka/Kb build."""
+    _check_device(eri_device)
+    m = _lib.MoleculeArgs(config, basis_set, param_path)
+    o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
+                     fp32_threshold)
+    K = ctypes.c_int()
+    check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
+    K = K.value
+    a0 = b0 = None
+    if set_initial_density:
+        a0 = np.ascontiguousarray(Pa0, dtype=np.float64).reshape(-1)
+        b0 = np.ascontiguousarray(Pb0, dtype=np.float64).reshape(-1)
+        if a0.size != K * K or b0.size != K * K:
+            raise HfxError(1, "initial density matrix dimension inconsistent with basis size")
+    r = _lib.ScfResult()
+    Pa, Pb, ea, eb = np.zeros((K, K)), np.zeros((K, K)), np.zeros(K), np.zeros(K)
+    st = lib.hfx_uhf_diis(m.ref(), ctypes.byref(o), int(spin_occ[0]), int(spin_occ[1]), ptr(a0), ptr(b0),
+                          ctypes.byref(r), ptr(Pa), ptr(Pb), ptr(ea), ptr(eb))
+    if st != 0 and not (st == 6 and not raise_on_nonconvergence):
+        check(st)
+    return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
+                K=r.K, Pa=Pa, Pb=Pb, Ea=ea, Eb=eb, duration=r.seconds, fock_ms=r.fock_ms,
+                fock_builds=r.fock_builds, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
+                BasisSet=basis_set, charge=charge)
+
+
+def one_electron(config, basis_set, param_path=None):
+    """(S, T, V) of the molecule (integrals.hpp:10-536), host."""
+    m = _lib.MoleculeArgs(config, basis_set, param_path)
+    K = ctypes.c_int()
+    check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
+    K = K.value
+    S, T, Vm = np.zeros((K, K)), np.zeros((K, K)), np.zeros((K, K))
+    check(lib.hfx_one_electron(m.ref(), ptr(S), ptr(T), ptr(Vm), None))
+    return S, T, Vm
+
+
+def measure_peaks(device=0):
+    """FP64 and FP32 FMA-loop GFLOP/s of the device."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    check(lib.hfx_measure_peaks(device, ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value

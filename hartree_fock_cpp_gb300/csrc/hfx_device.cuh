@@ -1,0 +1,86 @@
+// hfx_device.cuh -- device-side data layout and helpers shared by the
+// shell-quartet kernels.
+//
+// HBM layout of one job (all arrays device-resident for the job's lifetime):
+//   DPair[npairs]    one record per shell pair (A >= B in shell order), the
+//                    shell with the higher L stored first ("0" side)
+//   pp_geo[npp]      double4 per primitive pair: (p, Px, Py, Pz)
+//   E pool           per primitive pair, the dense Hermite->Cartesian matrix
+//                    E[ab][tuv] (n0*n1 x H(l0+l1)), with the primitive weights
+//                    w_i(a) w_j(b) (coefficient x cart_norm) and
+//                    exp(-mu |AB|^2) folded in; tuv in the reference's packed
+//                    order (integrals.hpp:343-358)
+//   Qbf[K(K+1)/2]    BF-level Schwarz bounds, pair_index order
+//   boys table       F_m(T_k), T_k = k/16, m = 0..kBoysM-1
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hfx {
+
+constexpr int kBoysM = 20;          // orders stored (12 + 7 Taylor terms + 1)
+constexpr int kBoysInvStep = 16;    // grid step 1/16
+constexpr int kBoysTMax = 36;       // table covers [0, 36]; upward recursion beyond
+constexpr int kBoysN = kBoysTMax * kBoysInvStep + 1;
+
+struct __align__(16) DPair {
+    int bf0, bf1;    // first basis function of shell 0 / shell 1
+    int l0, l1;      // l0 >= l1
+    int pp0, npp;    // primitive-pair range
+    long long e_off; // offset of the first E block (elements)
+    int same;        // shell 0 == shell 1
+    int id;          // pair id (index in the pair array)
+    double qmax;     // max_ab sqrt((ab|ab)) over the pair's BF pairs
+};
+
+__host__ __device__ constexpr int dncart(int l) { return (l + 1) * (l + 2) / 2; }
+__host__ __device__ constexpr int dnherm(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
+
+// packed Hermite index of (t,u,v), the reference's packed_r_index_cpu
+// (integrals.hpp:343-358): s-major, then t, then u.
+__host__ __device__ inline int herm_index(int t, int u, int v)
+{
+    int s = t + u + v;
+    int off = s * (s + 1) * (s + 2) / 6;
+    // sum_{aa<t} (s - aa + 1) = t*(s+1) - t*(t-1)/2
+    off += t * (s + 1) - t * (t - 1) / 2;
+    return off + u;
+}
+
+enum DigestMode { MODE_JK = 0, MODE_ERI = 1, MODE_SCHWARZ = 2 };
+
+struct Task {
+    int bra, ket;
+};
+
+// Work-list descriptor of one launch.
+struct LaunchArgs {
+    const DPair* pairs;
+    const double4* pp_geo;
+    const double* epool;
+    const float4* pp_geo32;
+    const float* epool32;
+    const double* boys;      // [kBoysN][kBoysM]
+    const float* boys32;
+    const Task* tasks;
+    int ntasks;
+    int* counter;            // work-queue head (zeroed before launch)
+    int K;
+    double thr;              // BF-level Schwarz threshold (< 0: none)
+    const double* Qbf;
+    // MODE_JK
+    const double* Dj;        // density for J (RHF: P; UHF: Pa+Pb)
+    const double* Dk;        // density for K (RHF: P; UHF: Pa)
+    const double* Dk2;       // UHF: Pb (nullptr for RHF)
+    double* Jacc;
+    double* Kacc;
+    double* Kacc2;
+    // MODE_ERI
+    double* eri;
+    // MODE_SCHWARZ
+    double* Qout_bf;
+    unsigned long long* Qout_sh;
+};
+
+}  // namespace hfx

@@ -1,0 +1,377 @@
+// hfx_engine.cpp -- host side of the device-resident job.
+//
+// Job creation replaces what the reference does per SCF inside ERI_GPU
+// (cuda/src/eri.cu:20-89): instead of an AoS of basis functions plus a
+// CPU-side Schwarz table, the job keeps in HBM
+//   * one record per shell pair with its primitive-pair geometry and the
+//     dense Hermite->Cartesian E matrices (weights and exp(-mu AB^2) folded),
+//   * a Boys-function table (FP64, Taylor grid),
+//   * the BF-level Schwarz table, computed on the device from the diagonal
+//     shell quartets (the reference's schwarz_bounds, integrals.hpp:732-752,
+//     runs on the CPU even on its GPU path, eri.cu:32),
+//   * the screened list of unique shell quartets (the reference screens per
+//     basis-function quartet, integrals.hpp:771),
+// so that every Fock build is: upload density -> one work-queue launch ->
+// symmetrise -> download, with no ERI storage.
+#include "hfx_engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace hfx {
+
+void cuda_check(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        hfx_status code = (e == cudaErrorMemoryAllocation) ? HFX_ERR_OOM : HFX_ERR_CUDA;
+        throw Error(code, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+static double flops_per_prim(int la, int lb, int lc, int ld)
+{
+    // algorithmic MD flop count per primitive quartet (boys + R + ket + bra + prefactor)
+    int L1 = la + lb, L2 = lc + ld, L = L1 + L2;
+    double boys = 12 + 3 * L;
+    double R = 3.0 * (L + 1) * (L + 2) * (L + 3) * (L + 4) / 24.0;
+    double ket = 2.0 * nherm(L1) * nherm(L2) * ncart(lc) * ncart(ld);
+    double bra = 2.0 * nherm(L1) * ncart(la) * ncart(lb) * ncart(lc) * ncart(ld);
+    return boys + R + ket + bra + 20;
+}
+
+Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
+{
+    if (opt_.screening_threshold == 0.0) opt_.screening_threshold = 1e-8;
+    if (opt_.fp32_threshold == 0.0) opt_.fp32_threshold = 1e-7;
+    device_ = opt_.device;
+    int ndev = 0;
+    cuda_check(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (device_ < 0 || device_ >= ndev) throw Error(HFX_ERR_INVALID, "invalid CUDA device ordinal");
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    cuda_check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, device_), "SM count");
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaEventCreate(&ev0_), "event");
+    cuda_check(cudaEventCreate(&ev1_), "event");
+    d_counter_.alloc(4);
+
+    // Boys table F_m(k/16), m < kBoysM
+    std::vector<double> tab((size_t)kBoysN * kBoysM);
+    for (int k = 0; k < kBoysN; ++k)
+        for (int m = 0; m < kBoysM; ++m) tab[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
+    d_boys_.upload(tab, stream_);
+
+    build_pairs();
+    compute_schwarz();
+    std::vector<Task> tasks;
+    build_tasks(opt_.screening_threshold, tasks, maxacc_, maxw_, maxr_);
+    ntasks_ = (int)tasks.size();
+    d_tasks_.upload(tasks, stream_);
+    cuda_check(cudaStreamSynchronize(stream_), "job setup");
+}
+
+Job::~Job()
+{
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    if (ev0_) cudaEventDestroy(ev0_);
+    if (ev1_) cudaEventDestroy(ev1_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+PairData build_pair_data(const Basis& basis)
+{
+    const auto& sh = basis.shells;
+    int ns = (int)sh.size();
+    PairData pd;
+    std::vector<double> Ex, Ey, Ez;
+    for (int A = 0; A < ns; ++A)
+        for (int B = 0; B <= A; ++B) {
+            int s0 = A, s1 = B;
+            if (sh[A].L < sh[B].L) std::swap(s0, s1);
+            const Shell& S0 = sh[s0];
+            const Shell& S1 = sh[s1];
+            int l0 = S0.L, l1 = S1.L, L = l0 + l1;
+            int n0 = ncart(l0), n1 = ncart(l1), H = nherm(L);
+            HostPair hp;
+            hp.s0 = s0;
+            hp.s1 = s1;
+            hp.l0 = l0;
+            hp.l1 = l1;
+            hp.same = (A == B);
+            hp.pp0 = (int)pd.geo.size();
+            hp.e_off = (long long)pd.epool.size();
+            int npp = 0;
+            int nt = L + 1;
+            for (int i = 0; i < S0.nprim(); ++i)
+                for (int j = 0; j < S1.nprim(); ++j) {
+                    double a = S0.exps[i], be = S1.exps[j], p = a + be;
+                    hermite_1d(l0, l1, a, be, S0.x, S1.x, Ex);
+                    hermite_1d(l0, l1, a, be, S0.y, S1.y, Ey);
+                    hermite_1d(l0, l1, a, be, S0.z, S1.z, Ez);
+                    pd.geo.push_back(make_double4(p, (a * S0.x + be * S1.x) / p, (a * S0.y + be * S1.y) / p,
+                                                  (a * S0.z + be * S1.z) / p));
+                    size_t base = pd.epool.size();
+                    pd.epool.resize(base + (size_t)n0 * n1 * H, 0.0);
+                    for (int c0 = 0; c0 < n0; ++c0) {
+                        int ax, ay, az;
+                        component(l0, c0, ax, ay, az);
+                        for (int c1 = 0; c1 < n1; ++c1) {
+                            int bx, by, bz;
+                            component(l1, c1, bx, by, bz);
+                            double w = S0.w[(size_t)c0 * S0.nprim() + i] * S1.w[(size_t)c1 * S1.nprim() + j];
+                            double* row = pd.epool.data() + base + (size_t)(c0 * n1 + c1) * H;
+                            for (int t = 0; t <= ax + bx; ++t)
+                                for (int u = 0; u <= ay + by; ++u)
+                                    for (int v = 0; v <= az + bz; ++v)
+                                        row[herm_index(t, u, v)] = w * Ex[((size_t)ax * (l1 + 1) + bx) * nt + t] *
+                                                                   Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
+                                                                   Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
+                        }
+                    }
+                    ++npp;
+                }
+            hp.npp = npp;
+            DPair d{};
+            d.bf0 = S0.bf0;
+            d.bf1 = S1.bf0;
+            d.l0 = l0;
+            d.l1 = l1;
+            d.pp0 = hp.pp0;
+            d.npp = npp;
+            d.e_off = hp.e_off;
+            d.same = hp.same ? 1 : 0;
+            d.id = (int)pd.hpairs.size();
+            d.qmax = 0.0;
+            pd.dpairs.push_back(d);
+            pd.hpairs.push_back(hp);
+        }
+    return pd;
+}
+
+void Job::build_pairs()
+{
+    PairData pd = build_pair_data(basis_);
+    hpairs_ = std::move(pd.hpairs);
+    d_pairs_.upload(pd.dpairs, stream_);
+    d_ppgeo_.upload(pd.geo, stream_);
+    d_epool_.upload(pd.epool, stream_);
+    cuda_check(cudaStreamSynchronize(stream_), "pair upload");
+}
+
+LaunchArgs Job::base_args() const
+{
+    LaunchArgs a{};
+    a.pairs = d_pairs_.p;
+    a.pp_geo = d_ppgeo_.p;
+    a.epool = d_epool_.p;
+    a.boys = d_boys_.p;
+    a.counter = d_counter_.p;
+    a.K = basis_.K;
+    a.thr = opt_.screening_threshold;
+    a.Qbf = d_qbf_.p;
+    return a;
+}
+
+void Job::run_tasks(int mode, int nk, const std::vector<Task>*, const DevBuf<Task>& tasks, int ntasks, int maxacc,
+                    int maxw, int maxr, LaunchArgs a)
+{
+    if (ntasks == 0) return;
+    a.tasks = tasks.p;
+    a.ntasks = ntasks;
+    cuda_check(cudaMemsetAsync(d_counter_.p, 0, sizeof(int), stream_), "memset counter");
+    size_t sm = generic_smem_bytes(maxacc, maxw, maxr);
+    int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (220 * 1024) / std::max<size_t>(sm, 1)));
+    int grid = std::min(ntasks, nsm_ * per_sm);
+    cuda_check(launch_generic(mode, nk, a, maxacc, maxw, maxr, grid, stream_), "quartet kernel launch");
+}
+
+void Job::compute_schwarz()
+{
+    int np = (int)hpairs_.size();
+    std::vector<Task> t(np);
+    int maxacc = 0, maxw = 0, maxr = 0;
+    for (int p = 0; p < np; ++p) {
+        t[p] = {p, p};
+        int L = hpairs_[p].l0 + hpairs_[p].l1;
+        int nab = ncart(hpairs_[p].l0) * ncart(hpairs_[p].l1);
+        maxacc = std::max(maxacc, nab * nab);
+        maxw = std::max(maxw, nherm(L) * nab);
+        maxr = std::max(maxr, nherm(2 * L));
+    }
+    DevBuf<Task> dt;
+    dt.upload(t, stream_);
+    size_t npair_bf = (size_t)basis_.K * (basis_.K + 1) / 2;
+    d_qbf_.alloc(npair_bf);
+    d_qsh_.alloc(np);
+    cuda_check(cudaMemsetAsync(d_qbf_.p, 0, npair_bf * sizeof(double), stream_), "memset");
+    cuda_check(cudaMemsetAsync(d_qsh_.p, 0, np * sizeof(unsigned long long), stream_), "memset");
+    LaunchArgs a = base_args();
+    a.thr = -1.0;
+    a.Qout_bf = d_qbf_.p;
+    a.Qout_sh = d_qsh_.p;
+    run_tasks(MODE_SCHWARZ, 1, &t, dt, np, maxacc, maxw, maxr, a);
+    qbf_.resize(npair_bf);
+    std::vector<unsigned long long> qs(np);
+    cuda_check(cudaMemcpyAsync(qbf_.data(), d_qbf_.p, npair_bf * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+               "download Q");
+    cuda_check(cudaMemcpyAsync(qs.data(), d_qsh_.p, np * sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream_),
+               "download Q");
+    cuda_check(cudaStreamSynchronize(stream_), "schwarz");
+    qsh_.resize(np);
+    for (int p = 0; p < np; ++p) {
+        double v;
+        std::memcpy(&v, &qs[p], sizeof(double));
+        qsh_[p] = v;
+    }
+}
+
+void Job::schwarz_host(std::vector<double>& Q) const { Q = qbf_; }
+
+void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr) const
+{
+    int np = (int)hpairs_.size();
+    // order pairs so that the pair with the larger (L, l0) is the bra
+    auto key = [&](int p) { return (hpairs_[p].l0 + hpairs_[p].l1) * 16 + hpairs_[p].l0; };
+    std::vector<double> cost;
+    tasks.clear();
+    maxacc = maxw = maxr = 1;
+    for (int X = 0; X < np; ++X)
+        for (int Y = 0; Y <= X; ++Y) {
+            if (thr >= 0.0 && qsh_[X] * qsh_[Y] < thr) continue;
+            int bra = X, ket = Y;
+            if (key(Y) > key(X)) std::swap(bra, ket);
+            tasks.push_back({bra, ket});
+        }
+    std::vector<double> c(tasks.size());
+    for (size_t t = 0; t < tasks.size(); ++t) {
+        const HostPair& b = hpairs_[tasks[t].bra];
+        const HostPair& k = hpairs_[tasks[t].ket];
+        c[t] = (double)b.npp * k.npp * flops_per_prim(b.l0, b.l1, k.l0, k.l1);
+        int L1 = b.l0 + b.l1, L2 = k.l0 + k.l1;
+        int nab = ncart(b.l0) * ncart(b.l1), ncd = ncart(k.l0) * ncart(k.l1);
+        maxacc = std::max(maxacc, nab * ncd);
+        maxw = std::max(maxw, nherm(L1) * ncd);
+        maxr = std::max(maxr, nherm(L1 + L2));
+    }
+    std::vector<size_t> idx(tasks.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return c[x] > c[y]; });
+    std::vector<Task> sorted(tasks.size());
+    for (size_t t = 0; t < idx.size(); ++t) sorted[t] = tasks[idx[t]];
+    tasks.swap(sorted);
+}
+
+void Job::fock_rhf_device(const double* dP, double* dG)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    int K = basis_.K;
+    size_t n = (size_t)K * K;
+    d_J_.alloc(n);
+    d_K_.alloc(n);
+    cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
+    LaunchArgs a = base_args();
+    a.Dj = dP;
+    a.Dk = dP;
+    a.Jacc = d_J_.p;
+    a.Kacc = d_K_.p;
+    cuda_check(cudaEventRecord(ev0_, stream_), "event");
+    run_tasks(MODE_JK, 1, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
+    cuda_check(cudaEventRecord(ev1_, stream_), "event");
+    cuda_check(cudaStreamSynchronize(stream_), "fock build");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    stats.ms = ms;
+    stats.quartets = ntasks_;
+    stats.launches = 2;
+}
+
+void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    int K = basis_.K;
+    size_t n = (size_t)K * K;
+    d_J_.alloc(n);
+    d_K_.alloc(n);
+    d_K2_.alloc(n);
+    d_Dj_.alloc(n);
+    cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaMemsetAsync(d_K2_.p, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaEventRecord(ev0_, stream_), "event");
+    cuda_check(launch_add(dPa, dPb, d_Dj_.p, (int)n, stream_), "add");
+    LaunchArgs a = base_args();
+    a.Dj = d_Dj_.p;
+    a.Dk = dPa;
+    a.Dk2 = dPb;
+    a.Jacc = d_J_.p;
+    a.Kacc = d_K_.p;
+    a.Kacc2 = d_K2_.p;
+    run_tasks(MODE_JK, 2, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    cuda_check(launch_finish_uhf(d_J_.p, d_K_.p, d_K2_.p, dJ, dKa, dKb, K, stream_), "finish");
+    cuda_check(cudaEventRecord(ev1_, stream_), "event");
+    cuda_check(cudaStreamSynchronize(stream_), "fock build");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    stats.ms = ms;
+    stats.quartets = ntasks_;
+    stats.launches = 3;
+}
+
+void Job::fock_rhf(const double* P, double* G)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    size_t n = (size_t)basis_.K * basis_.K;
+    d_D_.alloc(n);
+    d_out1_.alloc(n);
+    cuda_check(cudaMemcpyAsync(d_D_.p, P, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
+    fock_rhf_device(d_D_.p, d_out1_.p);
+    cuda_check(cudaMemcpyAsync(G, d_out1_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaStreamSynchronize(stream_), "D2H");
+}
+
+void Job::fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    size_t n = (size_t)basis_.K * basis_.K;
+    d_D_.alloc(n);
+    d_D2_.alloc(n);
+    d_out1_.alloc(n);
+    d_out2_.alloc(n);
+    d_out3_.alloc(n);
+    cuda_check(cudaMemcpyAsync(d_D_.p, Pa, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
+    cuda_check(cudaMemcpyAsync(d_D2_.p, Pb, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
+    fock_uhf_device(d_D_.p, d_D2_.p, d_out1_.p, d_out2_.p, d_out3_.p);
+    cuda_check(cudaMemcpyAsync(J, d_out1_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaMemcpyAsync(Ka, d_out2_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaMemcpyAsync(Kb, d_out3_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaStreamSynchronize(stream_), "D2H");
+}
+
+void Job::eri_unique(double thr, double* out)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    size_t P = (size_t)basis_.K * (basis_.K + 1) / 2;
+    size_t nq = P * (P + 1) / 2;
+    DevBuf<double> d_out;
+    d_out.alloc(nq);
+    cuda_check(cudaMemsetAsync(d_out.p, 0, nq * sizeof(double), stream_), "memset");
+    std::vector<Task> tasks;
+    int maxacc, maxw, maxr;
+    // every quartet whose shell-level bound can pass the BF-level test
+    build_tasks(thr, tasks, maxacc, maxw, maxr);
+    DevBuf<Task> dt;
+    dt.upload(tasks, stream_);
+    LaunchArgs a = base_args();
+    a.thr = thr;
+    a.eri = d_out.p;
+    run_tasks(MODE_ERI, 1, &tasks, dt, (int)tasks.size(), maxacc, maxw, maxr, a);
+    cuda_check(cudaMemcpyAsync(out, d_out.p, nq * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
+    cuda_check(cudaStreamSynchronize(stream_), "eri_unique");
+}
+
+}  // namespace hfx

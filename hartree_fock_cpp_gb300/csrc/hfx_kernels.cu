@@ -1,0 +1,334 @@
+// hfx_kernels.cu -- shell-quartet McMurchie-Davidson ERI kernels with
+// direct J/K digestion (sm_103a).
+//
+// Reference behaviour replaced: the reference evaluates one basis-function
+// quartet per CUDA block (cuda/include/kernels.cuh:84-168), recomputing the
+// Hermite E coefficients six times and the whole R recursion per (t,u,v) for
+// every primitive quartet (recursion.cuh:145-240), stores the full unique-ERI
+// tensor and contracts it with the density on the host every iteration
+// (linalg.hpp:100-129).  Here one CTA evaluates a whole *shell* quartet:
+//   stage 1  Boys F_m(T) (table + Taylor) and the R_{tuv} recursion, once per
+//            primitive quartet, level-parallel across a warp;
+//   stage 2  ket transform  W[tuv][cd] = sum_tnp (-1)^|tnp| R[tuv+tnp] E_cd[tnp]
+//   stage 3  bra transform  acc[ab][cd] += sum_tuv E_ab[tuv] W[tuv][cd]
+// and the finished Cartesian block is digested into J and K (8-fold
+// permutational symmetry, BF-level Schwarz mask as integrals.hpp:771), so the
+// ERI tensor is never stored.
+#include <cuda_runtime.h>
+
+#include "hfx_device.cuh"
+
+namespace hfx {
+
+__device__ __forceinline__ double boys_tab(int m, double T, const double* __restrict__ tab)
+{
+    if (T < (double)kBoysTMax) {
+        int k = __double2int_rn(T * kBoysInvStep);
+        double d = T - k * (1.0 / kBoysInvStep);
+        const double* f = tab + k * kBoysM + m;
+        double nd = -d;
+        // Taylor series in -d with coefficients F_{m+j}(T_k) / j!, j = 0..6
+        double r = __ldg(f + 6) * (1.0 / 720.0);
+        r = fma(r, nd, __ldg(f + 5) * (1.0 / 120.0));
+        r = fma(r, nd, __ldg(f + 4) * (1.0 / 24.0));
+        r = fma(r, nd, __ldg(f + 3) * (1.0 / 6.0));
+        r = fma(r, nd, __ldg(f + 2) * 0.5);
+        r = fma(r, nd, __ldg(f + 1));
+        r = fma(r, nd, __ldg(f + 0));
+        return r;
+    }
+    // large T: F_0 = sqrt(pi/T)/2 (erf(sqrt T) = 1 to double precision),
+    // stable upward recursion F_{j+1} = ((2j+1) F_j - e^{-T}) / (2T).
+    double F = 0.5 * sqrt(3.141592653589793 / T);
+    double e = exp(-T);
+    double inv2T = 0.5 / T;
+    for (int j = 0; j < m; ++j) F = ((2 * j + 1) * F - e) * inv2T;
+    return F;
+}
+
+// Inverse of herm_index: packed Hermite index -> (t,u,v,s) packed in an int.
+__device__ inline int herm_comp(int e)
+{
+    int s = 0;
+    while (dnherm(s) <= e) ++s;
+    int o = e - (s == 0 ? 0 : dnherm(s - 1));
+    int t = 0;
+    while (true) {
+        int width = s - t + 1;  // number of u values for this t
+        if (o < width) break;
+        o -= width;
+        ++t;
+    }
+    int u = o, v = s - t - u;
+    return t | (u << 8) | (v << 16) | (s << 24);
+}
+
+// Stage 1 on one warp: R^{(0)}_{tuv} (scaled by the ERI prefactor) for all
+// t+u+v <= L into the returned buffer (one of bufA / bufB).
+__device__ double* hermite_R_warp(double p, double Px, double Py, double Pz, double q, double Qx, double Qy,
+                                  double Qz, int L, double* bufA, double* bufB, double* seeds,
+                                  const short* idx3, const int* comp, const double* __restrict__ boys)
+{
+    const int lane = threadIdx.x & 31;
+    double X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+    double pq = p + q;
+    double rho = p * q / pq;
+    double T = rho * (X * X + Y * Y + Z * Z);
+    // 2 pi^{5/2} / (p q sqrt(p+q))  (integrals.hpp:698)
+    double pref = 34.98683665524972 / (p * q * sqrt(pq));
+    if (lane <= L) {
+        double F = boys_tab(lane, T, boys);
+        double m2r = -2.0 * rho, pw = 1.0;
+        for (int j = 0; j < lane; ++j) pw *= m2r;
+        seeds[lane] = pref * pw * F;
+    }
+    __syncwarp();
+    double* prev = bufA;
+    double* cur = bufB;
+    if (lane == 0) prev[0] = seeds[L];
+    __syncwarp();
+    for (int n = L - 1; n >= 0; --n) {
+        int top = L - n;
+        int cnt = dnherm(top);
+        for (int e = lane; e < cnt; e += 32) {
+            double val;
+            if (e == 0) {
+                val = seeds[n];
+            } else {
+                int c = comp[e];
+                int t = c & 255, u = (c >> 8) & 255, v = (c >> 16) & 255;
+                if (t > 0) {
+                    val = X * prev[idx3[((t - 1) * 13 + u) * 13 + v]];
+                    if (t > 1) val += (t - 1) * prev[idx3[((t - 2) * 13 + u) * 13 + v]];
+                } else if (u > 0) {
+                    val = Y * prev[idx3[(t * 13 + u - 1) * 13 + v]];
+                    if (u > 1) val += (u - 1) * prev[idx3[(t * 13 + u - 2) * 13 + v]];
+                } else {
+                    val = Z * prev[idx3[(t * 13 + u) * 13 + v - 1]];
+                    if (v > 1) val += (v - 1) * prev[idx3[(t * 13 + u) * 13 + v - 2]];
+                }
+            }
+            cur[e] = val;
+        }
+        __syncwarp();
+        double* tmp = prev;
+        prev = cur;
+        cur = tmp;
+    }
+    return prev;
+}
+
+__device__ __forceinline__ long long pair_idx(int a, int b)
+{
+    int hi = a > b ? a : b, lo = a > b ? b : a;
+    return (long long)hi * (hi + 1) / 2 + lo;
+}
+
+// Generic shell-quartet kernel: one CTA (128 threads) per shell quartet,
+// quartets taken from a global work queue.  MODE selects the digestion;
+// NK = 1 (RHF: J, K) or 2 (UHF: J, Ka, Kb).
+template <int MODE, int NK>
+__global__ void __launch_bounds__(128) k_quartet_generic(LaunchArgs a, int maxacc, int maxw, int maxr)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    short* idx3 = reinterpret_cast<short*>(smem);            // 13^3 shorts
+    int* comp = reinterpret_cast<int*>(smem + 4400);         // 455 ints
+    double* dbuf = reinterpret_cast<double*>(smem + 6240);
+    double* acc = dbuf;
+    double* W = acc + maxacc;
+    double* Ra = W + maxw;
+    double* Rb = Ra + maxr;
+    double* seeds = Rb + maxr;                               // 16
+    __shared__ int s_task;
+
+    for (int e = threadIdx.x; e < 13 * 13 * 13; e += blockDim.x) {
+        int t = e / 169, u = (e / 13) % 13, v = e % 13;
+        idx3[e] = (t + u + v <= 12) ? (short)herm_index(t, u, v) : (short)-1;
+    }
+    for (int e = threadIdx.x; e < 455; e += blockDim.x) comp[e] = herm_comp(e);
+    __syncthreads();
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const double* __restrict__ epool = a.epool;
+
+    while (true) {
+        if (tid == 0) s_task = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int tk = s_task;
+        __syncthreads();
+        if (tk >= a.ntasks) break;
+        const Task task = a.tasks[tk];
+        const DPair bra = a.pairs[task.bra];
+        const DPair ket = a.pairs[task.ket];
+        const int L1 = bra.l0 + bra.l1, L2 = ket.l0 + ket.l1, L = L1 + L2;
+        const int n1 = dncart(bra.l1), n3 = dncart(ket.l1);
+        const int nab = dncart(bra.l0) * n1, ncd = dncart(ket.l0) * n3;
+        const int H1 = dnherm(L1), H2 = dnherm(L2);
+        const int nout = nab * ncd;
+        for (int e = tid; e < nout; e += blockDim.x) acc[e] = 0.0;
+
+        for (int ij = 0; ij < bra.npp; ++ij) {
+            const double4 g1 = a.pp_geo[bra.pp0 + ij];
+            const double* Eij = epool + bra.e_off + (long long)ij * nab * H1;
+            for (int kl = 0; kl < ket.npp; ++kl) {
+                const double4 g2 = a.pp_geo[ket.pp0 + kl];
+                const double* Ekl = epool + ket.e_off + (long long)kl * ncd * H2;
+                if (warp == 0)
+                    hermite_R_warp(g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w, L, Ra, Rb, seeds, idx3, comp,
+                                   a.boys);
+                __syncthreads();
+                const double* R = (L % 2 == 0) ? Ra : Rb;
+                // stage 2: ket transform
+                for (int e = tid; e < H1 * ncd; e += blockDim.x) {
+                    int tuv = e / ncd, cd = e - tuv * ncd;
+                    int c1 = comp[tuv];
+                    int t = c1 & 255, u = (c1 >> 8) & 255, v = (c1 >> 16) & 255;
+                    const double* Ec = Ekl + cd * H2;
+                    double s = 0.0;
+                    for (int tn = 0; tn < H2; ++tn) {
+                        int c2 = comp[tn];
+                        int tt = t + (c2 & 255), uu = u + ((c2 >> 8) & 255), vv = v + ((c2 >> 16) & 255);
+                        double r = R[idx3[(tt * 13 + uu) * 13 + vv]];
+                        double ev = __ldg(Ec + tn);
+                        s = ((c2 >> 24) & 1) ? fma(-r, ev, s) : fma(r, ev, s);
+                    }
+                    W[e] = s;
+                }
+                __syncthreads();
+                // stage 3: bra transform into the Cartesian block
+                for (int e = tid; e < nout; e += blockDim.x) {
+                    int ab = e / ncd, cd = e - ab * ncd;
+                    const double* Ea = Eij + ab * H1;
+                    double s = 0.0;
+                    for (int tuv = 0; tuv < H1; ++tuv) s = fma(__ldg(Ea + tuv), W[tuv * ncd + cd], s);
+                    acc[e] += s;
+                }
+                __syncthreads();
+            }
+        }
+
+        // digestion
+        for (int e = tid; e < nout; e += blockDim.x) {
+            int ab = e / ncd, cd = e - ab * ncd;
+            int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
+            int i = bra.bf0 + ia, j = bra.bf1 + ib, k = ket.bf0 + ic, l = ket.bf1 + id;
+            double v = acc[e];
+            if (MODE == MODE_SCHWARZ) {
+                if (ab == cd && (!bra.same || ia >= ib)) {
+                    double qv = sqrt(v > 0.0 ? v : 0.0);
+                    a.Qout_bf[pair_idx(i, j)] = qv;
+                    atomicMax(a.Qout_sh + task.bra, (unsigned long long)__double_as_longlong(qv));
+                }
+                continue;
+            }
+            if (bra.same && ia < ib) continue;
+            if (ket.same && ic < id) continue;
+            long long pij = pair_idx(i, j), pkl = pair_idx(k, l);
+            if (task.bra == task.ket && pij < pkl) continue;
+            if (a.thr >= 0.0 && a.Qbf[pij] * a.Qbf[pkl] < a.thr) continue;
+            if (MODE == MODE_ERI) {
+                long long hi = pij > pkl ? pij : pkl, lo = pij > pkl ? pkl : pij;
+                a.eri[hi * (hi + 1) / 2 + lo] = v;
+                continue;
+            }
+            double f = (i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0);
+            v *= f;
+            const int K = a.K;
+            atomicAdd(a.Jacc + (long long)i * K + j, a.Dj[(long long)k * K + l] * v);
+            atomicAdd(a.Jacc + (long long)k * K + l, a.Dj[(long long)i * K + j] * v);
+            atomicAdd(a.Kacc + (long long)i * K + k, a.Dk[(long long)j * K + l] * v);
+            atomicAdd(a.Kacc + (long long)j * K + l, a.Dk[(long long)i * K + k] * v);
+            atomicAdd(a.Kacc + (long long)i * K + l, a.Dk[(long long)j * K + k] * v);
+            atomicAdd(a.Kacc + (long long)j * K + k, a.Dk[(long long)i * K + l] * v);
+            if (NK == 2) {
+                atomicAdd(a.Kacc2 + (long long)i * K + k, a.Dk2[(long long)j * K + l] * v);
+                atomicAdd(a.Kacc2 + (long long)j * K + l, a.Dk2[(long long)i * K + k] * v);
+                atomicAdd(a.Kacc2 + (long long)i * K + l, a.Dk2[(long long)j * K + k] * v);
+                atomicAdd(a.Kacc2 + (long long)j * K + k, a.Dk2[(long long)i * K + l] * v);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// G = (Jacc + Jacc^T)/4 - 1/2 (Kacc + Kacc^T)/8   (RHF, linalg.hpp:100-129)
+__global__ void k_finish_rhf(const double* Jacc, const double* Kacc, double* G, int K)
+{
+    int n = K * K;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        int i = e / K, j = e - i * K;
+        double J = 0.25 * (Jacc[e] + Jacc[j * K + i]);
+        double X = 0.125 * (Kacc[e] + Kacc[j * K + i]);
+        G[e] = J - 0.5 * X;
+    }
+}
+
+// J = (Jacc + Jacc^T)/4, K = (Kacc + Kacc^T)/8  (UHF, linalg.hpp:215-296)
+__global__ void k_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
+                             double* Kbo, int K)
+{
+    int n = K * K;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        int i = e / K, j = e - i * K;
+        J[e] = 0.25 * (Jacc[e] + Jacc[j * K + i]);
+        Kao[e] = 0.125 * (Ka[e] + Ka[j * K + i]);
+        Kbo[e] = 0.125 * (Kb[e] + Kb[j * K + i]);
+    }
+}
+
+__global__ void k_add(const double* A, const double* B, double* C, int n)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) C[e] = A[e] + B[e];
+}
+
+// Host-side launch helpers (called from hfx_engine.cpp).
+size_t generic_smem_bytes(int maxacc, int maxw, int maxr)
+{
+    return 6240 + sizeof(double) * (size_t)(maxacc + maxw + 2 * maxr + 16);
+}
+
+cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
+                           cudaStream_t st)
+{
+    size_t sm = generic_smem_bytes(maxacc, maxw, maxr);
+    auto go = [&](auto kern) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, 128, sm, st>>>(a, maxacc, maxw, maxr);
+        return cudaGetLastError();
+    };
+    if (mode == MODE_SCHWARZ) return go(k_quartet_generic<MODE_SCHWARZ, 1>);
+    if (mode == MODE_ERI) return go(k_quartet_generic<MODE_ERI, 1>);
+    if (nk == 2) return go(k_quartet_generic<MODE_JK, 2>);
+    return go(k_quartet_generic<MODE_JK, 1>);
+}
+
+cudaError_t launch_finish_rhf(const double* Jacc, const double* Kacc, double* G, int K, cudaStream_t st)
+{
+    int n = K * K;
+    int grid = (n + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    k_finish_rhf<<<grid, 256, 0, st>>>(Jacc, Kacc, G, K);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
+                              double* Kbo, int K, cudaStream_t st)
+{
+    int n = K * K;
+    int grid = (n + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    k_finish_uhf<<<grid, 256, 0, st>>>(Jacc, Ka, Kb, J, Kao, Kbo, K);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add(const double* A, const double* B, double* C, int n, cudaStream_t st)
+{
+    int grid = (n + 255) / 256;
+    if (grid > 1024) grid = 1024;
+    k_add<<<grid, 256, 0, st>>>(A, B, C, n);
+    return cudaGetLastError();
+}
+
+}  // namespace hfx

@@ -1,0 +1,231 @@
+/*
+ * hfx.h -- C ABI of libhfx, the GB300 (sm_103a) direct-SCF Fock-build engine
+ * for the McMurchie-Davidson Hartree-Fock code KLYYCYNN/hartree_fock_cpp.
+ *
+ * The engine replaces the reference's ERI call and its per-iteration Fock
+ * contraction:
+ *   - std::vector<double> ERI_GPU(const std::vector<basis_function>&, double)
+ *       declared include/scf.hpp:41-44, defined cuda/src/eri.cu:20-89
+ *       -> hfx_eri_unique / hfx_eri_gpu (same packed eri_index layout)
+ *   - schwarz_bounds (include/integrals.hpp:732-752)      -> hfx_schwarz
+ *   - repulsion_matrix (include/linalg.hpp:100-129)       -> hfx_fock_rhf
+ *   - coulomb_matrix + 2x exchange_matrix
+ *       (include/linalg.hpp:215-296, called scf.hpp:542-544) -> hfx_fock_uhf
+ *   - rhf_diis / uhf_diis with eri_device "GPU"
+ *       (include/scf.hpp:205-419 / 423-682)              -> hfx_rhf_diis / hfx_uhf_diis
+ * J and K are built directly from shell-quartet ERIs; the ERI tensor is never
+ * stored (only hfx_eri_unique, the literal ERI_GPU replacement, writes it).
+ *
+ * Conventions: all matrices are K x K, row-major, double, in the reference's
+ * basis-function order (atoms -> CSV shells -> Cartesian components with lx
+ * outer, ly inner, as basis.hpp:52-64).  Buffers are caller-owned host memory
+ * unless a function name ends in _device.  Every function returns an
+ * hfx_status; no C++ exception crosses this boundary.  A job handle is used by
+ * one host thread at a time.  Errors never terminate the process (the
+ * reference calls std::exit from cuda_check, cuda/src/eri.cu:8-14).
+ */
+#ifndef HFX_H
+#define HFX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int hfx_status;
+
+enum {
+    HFX_OK = 0,
+    HFX_ERR_INVALID = 1,      /* bad argument, size or option */
+    HFX_ERR_BASIS = 2,        /* basis file missing / malformed / unsupported element or L */
+    HFX_ERR_CUDA = 3,         /* CUDA runtime error (message in hfx_last_error) */
+    HFX_ERR_OOM = 4,          /* device or host allocation failed / admission refused */
+    HFX_ERR_UNSUPPORTED = 5,  /* feature outside the engine's limits (e.g. L > 3) */
+    HFX_ERR_NOT_CONVERGED = 6,/* SCF reached max iterations (results still filled) */
+    HFX_ERR_CANCELLED = 7,    /* served job cancelled */
+    HFX_ERR_TIMEOUT = 8,      /* served job or bounded device wait timed out */
+    HFX_ERR_NUMERIC = 9       /* NaN/Inf in energy or Fock matrix */
+};
+
+/* Precision of the Fock build. */
+enum {
+    HFX_PREC_FP64 = 0,        /* every quartet in FP64 (the all-FP64 oracle path) */
+    HFX_PREC_MIXED = 1        /* quartets with Schwarz bound < fp32_threshold in FP32 */
+};
+
+/* ---- basis descriptions -------------------------------------------------- */
+
+/* Basis-function level description: exactly the reference's
+ * std::vector<basis_function> (include/types.hpp:16-29) flattened.
+ * Consecutive functions must form complete Cartesian shells in
+ * angmom_partition order (which basis_construction always produces). */
+typedef struct {
+    int K;                    /* number of basis functions */
+    const double *centres;    /* 3*K, bohr */
+    const int *lmn;           /* 3*K, (lx, ly, lz) */
+    const int *prim_offset;   /* K+1, range of each function's primitives */
+    const double *alpha;      /* exponents */
+    const double *coeff;      /* contraction coefficients */
+    const double *norm;       /* primitive norms (cart_norm, basis.hpp:28-49) */
+} hfx_functions;
+
+/* Molecule + basis-set name, built like basis_construction (basis.hpp:157-262). */
+typedef struct {
+    int natom;
+    const char *const *symbols;  /* element symbols, e.g. "O" */
+    const double *xyz;           /* 3*natom, bohr */
+    const char *basis_set;       /* "STO-3G", "6-31G", "6-31G*", "cc-pVDZ", "cc-pVTZ" */
+    const char *basis_path;      /* directory holding <set>/<El>.csv; NULL = bundled sets */
+} hfx_molecule;
+
+/* Engine options (zero-initialise, then set; 0 selects the default). */
+typedef struct {
+    double screening_threshold; /* BF-level Schwarz cut Q_ij*Q_kl < thr -> 0; default 1e-8
+                                   (run.hpp:46 / integrals.hpp:771); set < 0 for no screening */
+    int precision;              /* HFX_PREC_FP64 (default) or HFX_PREC_MIXED */
+    double fp32_threshold;      /* mixed: shell-quartet bound below this runs in FP32; default 1e-7 */
+    int device;                 /* CUDA device ordinal; default 0 */
+    int reserved[8];
+} hfx_options;
+
+typedef struct hfx_job hfx_job;
+
+/* Build a job from a basis-function list (drop-in for the reference's
+ * std::vector<basis_function>).  Uploads pair data, computes the Schwarz
+ * table on the device, and builds the screened shell-quartet work lists. */
+hfx_status hfx_create(const hfx_functions *basis, const hfx_options *opt, hfx_job **job);
+
+/* Same, building the basis from a molecule and a basis-set name. */
+hfx_status hfx_create_molecule(const hfx_molecule *mol, const hfx_options *opt, hfx_job **job);
+
+hfx_status hfx_destroy(hfx_job *job);
+
+/* Number of basis functions of the job. */
+hfx_status hfx_nbasis(const hfx_job *job, int *K);
+
+/* Export the job's basis-function list (sizes as in hfx_functions; pass
+ * NULL for any array not wanted; nprim_total receives the primitive count). */
+hfx_status hfx_export_functions(const hfx_job *job, double *centres, int *lmn, int *prim_offset,
+                                double *alpha, double *coeff, double *norm, int *nprim_total);
+
+/* Schwarz bounds Q_ij = sqrt(max((ij|ij),0)) for all K(K+1)/2 pairs in
+ * pair_index order (indexing.hpp:33-40); replaces schwarz_bounds
+ * (integrals.hpp:732-752). */
+hfx_status hfx_schwarz(hfx_job *job, double *Q);
+
+/* RHF two-electron matrix G = J[P] - 1/2 K[P] (linalg.hpp:100-129), P and G
+ * K x K host buffers.  Replaces repulsion_matrix(P, ERI). */
+hfx_status hfx_fock_rhf(hfx_job *job, const double *P, double *G);
+
+/* UHF: J = J[Pa+Pb], Ka = K[Pa], Kb = K[Pb] (linalg.hpp:215-296). */
+hfx_status hfx_fock_uhf(hfx_job *job, const double *Pa, const double *Pb, double *J, double *Ka,
+                        double *Kb);
+
+/* Device-pointer variants (K x K double buffers already on the job's device;
+ * run on the job's stream, synchronise before returning). */
+hfx_status hfx_fock_rhf_device(hfx_job *job, const double *dP, double *dG);
+hfx_status hfx_fock_uhf_device(hfx_job *job, const double *dPa, const double *dPb, double *dJ,
+                               double *dKa, double *dKb);
+
+/* All unique ERIs in the reference's packed layout: out[eri_index(i,j,k,l)],
+ * P(P+1)/2 doubles with P = K(K+1)/2, zero where Q_ij*Q_kl < threshold
+ * (integrals.hpp:754-787 / cuda/src/eri.cu:20-89). */
+hfx_status hfx_eri_unique(hfx_job *job, double threshold, double *out);
+
+/* One-shot literal ERI_GPU(basis, threshold) replacement. */
+hfx_status hfx_eri_gpu(const hfx_functions *basis, double threshold, double *out);
+
+/* Statistics of the last Fock build. */
+typedef struct {
+    double ms;                /* device time of the build (CUDA events) */
+    double quartets;          /* surviving shell quartets */
+    double quartets_fp32;     /* of which computed in FP32 */
+    double prim_quartets;     /* primitive quartets evaluated */
+    double flops_fp64;        /* algorithmic flops (MD count) done in FP64 */
+    double flops_fp32;        /* algorithmic flops done in FP32 */
+    int launches;             /* kernel launches of the build */
+    int reserved[7];
+} hfx_build_stats;
+
+hfx_status hfx_last_build_stats(const hfx_job *job, hfx_build_stats *stats);
+
+/* ---- SCF drivers (scf.hpp semantics) -------------------------------------- */
+
+typedef struct {
+    int max_iterations;         /* default 10000 (scf.hpp:213) */
+    double epsilon;             /* RMSD(P) and ||FPS-SPF|| threshold; default 1e-6 */
+    double damping;             /* default 0.3, first 3 iterations */
+    double screening_threshold; /* default 1e-8 */
+    double energy_threshold;    /* > 0 adds |E_n - E_{n-1}| < energy_threshold; default off */
+    int charge;
+    int precision;              /* HFX_PREC_FP64 / HFX_PREC_MIXED */
+    double fp32_threshold;      /* mixed precision cut (see hfx_options) */
+    int fp64_final_cycles;      /* mixed: rebuild incrementally in FP64 once RMSD(P) < 1e3*epsilon; default 1 (on) */
+    int start_diis;             /* default 4 (scf.hpp:235) */
+    int max_history;            /* default 8 (scf.hpp:236) */
+    int verbose;
+    int reserved[6];
+} hfx_scf_options;
+
+typedef struct {
+    double E_tot, E_ele, E_nuc;
+    int iterations;
+    int converged;
+    int K;
+    int n_electrons;
+    double seconds;             /* wall time of the whole SCF */
+    double fock_ms;             /* summed device time of the Fock builds */
+    int fock_builds;
+    int reserved[7];
+} hfx_scf_result;
+
+/* RHF (scf.hpp:205-419).  P0: optional K*K initial density (NULL = zero).
+ * density / coefficient / mo_energy: optional outputs (K*K, K*K, K). */
+hfx_status hfx_rhf_diis(const hfx_molecule *mol, const hfx_scf_options *opt, const double *P0,
+                        hfx_scf_result *res, double *density, double *coefficient, double *mo_energy);
+
+/* UHF (scf.hpp:423-682), n_alpha + n_beta electrons. */
+hfx_status hfx_uhf_diis(const hfx_molecule *mol, const hfx_scf_options *opt, int n_alpha, int n_beta,
+                        const double *Pa0, const double *Pb0, hfx_scf_result *res, double *Pa, double *Pb,
+                        double *mo_energy_a, double *mo_energy_b);
+
+/* The same drivers with a caller-supplied two-electron builder in place of
+ * the GPU engine: the host SCF loop (DIIS, eigensolver, convergence logic)
+ * can then be checked against another Fock builder, e.g. the reference's
+ * stored-tensor contraction.  A builder returns 0 on success. */
+typedef int (*hfx_g_builder)(void *user, const double *P, double *G);
+typedef int (*hfx_jk_builder)(void *user, const double *Pa, const double *Pb, double *J, double *Ka, double *Kb);
+hfx_status hfx_rhf_diis_with_builder(const hfx_molecule *mol, const hfx_scf_options *opt, const double *P0,
+                                     hfx_g_builder g, void *user, hfx_scf_result *res, double *density,
+                                     double *mo_energy);
+hfx_status hfx_uhf_diis_with_builder(const hfx_molecule *mol, const hfx_scf_options *opt, int n_alpha, int n_beta,
+                                     hfx_jk_builder jk, void *user, hfx_scf_result *res, double *Pa, double *Pb);
+
+/* Basis-function list of a molecule as the engine builds it (host only, no
+ * device work): K, then the hfx_functions arrays (sizes as there; pass NULL
+ * to query K and nprim_total first). */
+hfx_status hfx_build_functions(const hfx_molecule *mol, int *K, int *nprim_total, double *centres, int *lmn,
+                               int *prim_offset, double *alpha, double *coeff, double *norm);
+
+/* Host image of the per-shell-pair data the kernels read (no device work):
+ * for each shell pair p: rec[10*p..] = {bf0, bf1, l0, l1, pp0, npp, e_off_lo,
+ * e_off_hi, same, id}; geo[4*q..] = (p, Px, Py, Pz) per primitive pair q;
+ * epool = the dense E[ab][tuv] blocks.  Query sizes with NULL arrays. */
+hfx_status hfx_debug_pair_data(const hfx_molecule *mol, int *npairs, int *nprimpairs, long long *nepool, int *rec,
+                               double *geo, double *epool);
+
+/* One-electron matrices S, T, V of a molecule (integrals.hpp:10-536), host. */
+hfx_status hfx_one_electron(const hfx_molecule *mol, double *S, double *T, double *V, int *K);
+
+/* Last error message of the calling thread (empty if none). */
+hfx_status hfx_last_error(char *buf, size_t n);
+
+/* FP64 / FP32 FMA-loop peak of the device, GFLOP/s (roofline denominators). */
+hfx_status hfx_measure_peaks(int device, double *fp64_gflops, double *fp32_gflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HFX_H */

