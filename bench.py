@@ -1,0 +1,362 @@
+"""Benchmark of the direct-SCF Fock-build engine (one JSON line on rank 0).
+
+Workload (N=1): benzene RHF/cc-pVDZ (K=120, 21 doubly occupied), the FP64 GPU
+drop-in for the reference's ERI/Fock call, reference SCF settings with the
+stated convergence (DIIS 8, |dE| < 1e-8 Eh and RMS dD < 1e-7).  One step = one
+SCF solve from a zero density.
+
+  value  RHF solves/s with the job resident in HBM (basis, pair data, Schwarz
+         table and quartet lists uploaded before the timed region; each SCF
+         iteration moves only the K x K density / G through the C ABI)
+  e2e    RHF solves/s through hfx_rhf_diis (molecule in host memory: basis
+         construction, job setup, uploads, every SCF iteration, downloads)
+  extra  FP64 Fock builds/s of the device-pointer build, p50/p99 solve
+         latency, the roofline of the shell-quartet kernel against the
+         measured FP64 FMA-loop peak, and the reference-algorithm CPU baseline
+         timed on this host's cores on a bounded sample.
+
+--impl reference times the reference's CPU algorithm for the same workload
+(oracle port of integrals.hpp repulsion_tensor + linalg.hpp repulsion_matrix,
+all host threads, bounded sample per step, extrapolated to solves/s).
+Multi-GPU: replicas only (one independent solve stream per rank), launched
+with torchrun; value = solves of all ranks / max time.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "RHF solves/s"
+UNIT = "solves/s"
+WORKLOAD = "benzene RHF/cc-pVDZ, FP64 direct J/K (K=120, 21 occ), DIIS(8), |dE|<1e-8 & RMS dD<1e-7"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except Exception:
+                continue
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(torch, buf):
+    buf.zero_()
+
+
+def cpu_baseline(config, basis, iterations, sample_quartets, nthreads, seed=20261203):
+    """Reference algorithm (oracle port of integrals.hpp:754-787 + linalg.hpp:100-129)
+    on a bounded sample: time per unique BF quartet over the host threads and one
+    O(K^4) repulsion_matrix contraction; extrapolated to one SCF solve."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+    orc = O.Oracle(config, basis)
+    K = orc.K
+    npair = K * (K + 1) // 2
+    nq = npair * (npair + 1) // 2
+    t0 = time.perf_counter()
+    Q = orc.schwarz_bounds()
+    t_schwarz = time.perf_counter() - t0
+    rng = np.random.default_rng(seed)
+    qid = rng.integers(0, nq, size=sample_quartets)
+    # quartet id -> (i,j,k,l) as indexing.hpp:55-85
+    p1 = ((np.sqrt(8.0 * qid + 1.0) - 1.0) / 2.0).astype(np.int64)
+    p1 -= (p1 * (p1 + 1) // 2 > qid)
+    p1 += ((p1 + 1) * (p1 + 2) // 2 <= qid)
+    p2 = qid - p1 * (p1 + 1) // 2
+    def unpair(p):
+        a = ((np.sqrt(8.0 * p + 1.0) - 1.0) / 2.0).astype(np.int64)
+        a -= (a * (a + 1) // 2 > p)
+        a += ((a + 1) * (a + 2) // 2 <= p)
+        return a, p - a * (a + 1) // 2
+    i, j = unpair(p1)
+    k, l = unpair(p2)
+    ijkl = np.stack([i, j, k, l], 1).astype(np.int32)
+    surv = Q[p1] * Q[p2] >= 1e-8
+    t0 = time.perf_counter()
+    orc.eri_list(ijkl, bounds=Q, threshold=1e-8, nthreads=nthreads)
+    t_sample = time.perf_counter() - t0
+    frac = float(surv.mean())
+    t_tensor = t_schwarz + t_sample / sample_quartets * nq
+    P = np.eye(K)
+    eri_dummy = np.zeros(nq)
+    t0 = time.perf_counter()
+    O.repulsion_matrix(P, eri_dummy)
+    t_contract = time.perf_counter() - t0
+    t_solve = t_tensor + iterations * t_contract
+    return dict(value=1.0 / t_solve, unit=UNIT, cores=nthreads, kind="port",
+                sample="%d random unique BF quartets of %d (%.1f%% survive 1e-8 screening) on %d threads, "
+                       "plus one O(K^4) repulsion_matrix; extrapolated: tensor %.1f s + %d x %.2f s contraction"
+                       % (sample_quartets, nq, 100 * frac, nthreads, t_tensor, iterations, t_contract),
+                seconds_per_solve=t_solve, sample_seconds=t_sample + t_contract + t_schwarz)
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from hartree_fock_cpp_gb300 import workloads as W
+    nthreads = os.cpu_count() or 1
+    cfg = W.benzene()
+    iters = 14
+    vals = []
+    base = None
+    for s in range(args.warmup + args.steps):
+        b = cpu_baseline(cfg, "cc-pVDZ", iters, sample_quartets=max(400, 100 * nthreads), nthreads=nthreads,
+                         seed=20261203 + s)
+        if s >= args.warmup:
+            vals.append(b["seconds_per_solve"])
+            base = b
+    t = float(np.mean(vals))
+    v = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "impl": "reference CPU algorithm (oracle port), host threads"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": base["kind"],
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import torch
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    import hartree_fock_cpp_gb300 as H
+    from hartree_fock_cpp_gb300 import _lib, workloads as W
+
+    fp64_peak, fp32_peak = H.measure_peaks(local)
+    cfg = W.benzene()
+    basis = "cc-pVDZ"
+    scf_kw = dict(epsilon=1e-7, energy_threshold=1e-8)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    # ---- value: device-resident job, solves/s -------------------------------
+    fb = H.FockBuilder(config=cfg, basis_set=basis, device=local)
+    K = fb.K
+    mol = fb._mol
+    o = _lib.ScfOptions()
+    o.epsilon = scf_kw["epsilon"]
+    o.energy_threshold = scf_kw["energy_threshold"]
+    res = _lib.ScfResult()
+    dens = np.zeros((K, K))
+
+    def solve_resident():
+        st = _lib.lib.hfx_job_rhf(fb._job, ctypes.byref(o), None, ctypes.byref(res), _lib.ptr(dens), None, None)
+        _lib.check(st)
+        return res.iterations, res.fock_builds, res.E_tot
+
+    for _ in range(args.warmup):
+        solve_resident()
+    lat = []
+    iters = builds = 0
+    E_val = None
+    clocks = Clocks(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for _ in range(args.steps):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        it, nb, E_val = solve_resident()
+        e1.record()
+        torch.cuda.synchronize()
+        lat.append(e0.elapsed_time(e1))
+        iters, builds = it, nb
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    t_total = sum(lat) / 1e3
+    if ws > 1:
+        tt = torch.tensor([t_total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = ws * args.steps / t_total
+
+    # ---- Fock builds/s (device-pointer build) and the kernel roofline --------
+    rng = np.random.default_rng(0)
+    P = torch.tensor(dens if np.abs(dens).sum() > 0 else rng.normal(size=(K, K)), device="cuda",
+                     dtype=torch.float64)
+    G = torch.zeros_like(P)
+    for _ in range(2):
+        fb.repulsion_matrix_device(P.data_ptr(), G.data_ptr())
+    kms, bms = [], []
+    for _ in range(max(3, args.steps)):
+        flush_l2(torch, flush)
+        torch.cuda.synchronize()
+        fb.repulsion_matrix_device(P.data_ptr(), G.data_ptr())
+        s = fb.stats()
+        kms.append(s["kernel_ms"])
+        bms.append(s["ms"])
+    s = fb.stats()
+    kernel_ms = float(np.mean(kms))
+    build_ms = float(np.mean(bms))
+    flops = s["flops_fp64"]
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    peak = fp64_peak / 1e3
+
+    # ---- e2e: through hfx_rhf_diis with host buffers -------------------------
+    e2e_lat = []
+    r = None
+    for k in range(1 + max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        r = H.rhf_diis(cfg, basis, **scf_kw)
+        dt = time.perf_counter() - t0
+        if k > 0:
+            e2e_lat.append(dt)
+    e2e_t = float(np.mean(e2e_lat))
+    if ws > 1:
+        tt = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    m = H._lib.MoleculeArgs(cfg, basis)
+    npp = ctypes.c_int()
+    npr = ctypes.c_int()
+    nep = ctypes.c_longlong()
+    _lib.check(_lib.lib.hfx_debug_pair_data(m.ref(), ctypes.byref(npp), ctypes.byref(npr), ctypes.byref(nep), None,
+                                            None, None))
+    setup_bytes = nep.value * 8 + npr.value * 32 + npp.value * 48 + s["quartets"] * 8
+    h2d = int(setup_bytes + r["fock_builds"] * K * K * 8)
+    d2h = int(r["fock_builds"] * K * K * 8 + K * (K + 1) // 2 * 8 + npp.value * 8)
+
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.barrier()
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        b = cpu_baseline(cfg, basis, iters, sample_quartets=max(400, 100 * nthreads), nthreads=nthreads)
+        cpu = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_total / args.steps * 1e3 / max(1, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "molecule": "benzene D6h (C r=2.6379, H r=4.68 bohr)", "basis": basis,
+                   "K": K, "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between steps (512 MB)"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
+        "fock_builds_per_s": {"fp64": 1e3 / build_ms, "mixed": None},
+        "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured FP64 FMA-loop peak of this GPU (hfx_measure_peaks, same run)",
+                     "flops_per_launch": flops, "kernel_ms": kernel_ms, "fp32_peak_tflops": fp32_peak / 1e3},
+        "e2e": {"value": 1.0 / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(args.steps * builds * s["launches"]),
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+
+
+def run_fock_only(args):
+    """Small fixed case for profilers: one job, a few device Fock builds."""
+    import torch
+    import hartree_fock_cpp_gb300 as H
+    from hartree_fock_cpp_gb300 import workloads as W
+    cfg = getattr(W, args.molecule)()
+    prec = H.HFX_PREC_MIXED if args.precision == "mixed" else H.HFX_PREC_FP64
+    fb = H.FockBuilder(config=cfg, basis_set=args.basis, precision=prec)
+    K = fb.K
+    rng = np.random.default_rng(0)
+    P = rng.normal(size=(K, K)) * 0.1
+    P = torch.tensor(P + P.T, device="cuda", dtype=torch.float64)
+    G = torch.zeros_like(P)
+    for _ in range(args.builds):
+        fb.repulsion_matrix_device(P.data_ptr(), G.data_ptr())
+    s = fb.stats()
+    print(json.dumps({"molecule": args.molecule, "basis": args.basis, "K": K, "builds": args.builds,
+                      "last_build_ms": s["ms"], "kernel_ms": s["kernel_ms"], "flops": s["flops_fp64"],
+                      "quartets": s["quartets"]}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fock-only", action="store_true",
+                    help="profiling case: job setup + --builds device Fock builds of --molecule/--basis")
+    ap.add_argument("--molecule", default="benzene", choices=["water", "benzene", "n_decane"])
+    ap.add_argument("--basis", default="cc-pVDZ")
+    ap.add_argument("--builds", type=int, default=2)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    args = ap.parse_args()
+    if args.fock_only:
+        run_fock_only(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

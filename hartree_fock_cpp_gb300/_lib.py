@@ -43,7 +43,7 @@ class Options(ctypes.Structure):
 
 
 class BuildStats(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double), ("quartets", ctypes.c_double), ("quartets_fp32", ctypes.c_double),
+    _fields_ = [("ms", ctypes.c_double), ("kernel_ms", ctypes.c_double), ("quartets", ctypes.c_double), ("quartets_fp32", ctypes.c_double),
                 ("prim_quartets", ctypes.c_double), ("flops_fp64", ctypes.c_double),
                 ("flops_fp32", ctypes.c_double), ("launches", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
@@ -88,6 +88,8 @@ SIGNATURES = {
     "hfx_fock_uhf_device": (I, [V, V, V, V, V, V]),
     "hfx_eri_unique": (I, [V, D, V]),
     "hfx_eri_gpu": (I, [V, D, V]),
+    "hfx_job_rhf": (I, [V, V, V, V, V, V, V]),
+    "hfx_job_uhf": (I, [V, V, I, I, V, V, V, V, V]),
     "hfx_last_build_stats": (I, [V, V]),
     "hfx_rhf_diis": (I, [V, V, V, V, V, V, V]),
     "hfx_uhf_diis": (I, [V, V, I, I, V, V, V, V, V, V, V]),

@@ -11,6 +11,7 @@
 
 struct hfx_job {
     std::unique_ptr<hfx::Job> job;
+    std::unique_ptr<hfx::ScfSetup> setup;   // S, H, X, E_nuc; made on first SCF
 };
 
 namespace hfx {
@@ -165,8 +166,8 @@ hfx_status hfx_debug_pair_data(const hfx_molecule* mol, int* npairs, int* nprimp
             }
         if (geo)
             for (size_t q = 0; q < pd.geo.size(); ++q) {
-                geo[4 * q] = pd.geo[q].x; geo[4 * q + 1] = pd.geo[q].y;
-                geo[4 * q + 2] = pd.geo[q].z; geo[4 * q + 3] = pd.geo[q].w;
+                geo[4 * q] = pd.geo[q].p; geo[4 * q + 1] = pd.geo[q].x;
+                geo[4 * q + 2] = pd.geo[q].y; geo[4 * q + 3] = pd.geo[q].z;
             }
         if (epool) std::memcpy(epool, pd.epool.data(), pd.epool.size() * sizeof(double));
     });
@@ -316,6 +317,61 @@ hfx_status hfx_uhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, int
         if (Pb) std::memcpy(Pb, out.P2.data(), sizeof(double) * K * K);
         if (mo_energy_a && !out.e.empty()) std::memcpy(mo_energy_a, out.e.data(), sizeof(double) * K);
         if (mo_energy_b && !out.e2.empty()) std::memcpy(mo_energy_b, out.e2.data(), sizeof(double) * K);
+        if (!out.converged) throw Error(HFX_ERR_NOT_CONVERGED, "SCF did not converge within max_iterations");
+    });
+}
+
+static const ScfSetup& job_setup(hfx_job* job)
+{
+    if (job->job->basis().atom_Z.empty())
+        throw Error(HFX_ERR_INVALID, "SCF needs a job created from a molecule (nuclear charges)");
+    if (!job->setup) job->setup = std::make_unique<ScfSetup>(scf_setup(job->job->basis()));
+    return *job->setup;
+}
+
+hfx_status hfx_job_rhf(hfx_job* job, const hfx_scf_options* opt, const double* P0, hfx_scf_result* res,
+                       double* density, double* coefficient, double* mo_energy)
+{
+    return guarded([&] {
+        if (!job) throw Error(HFX_ERR_INVALID, "null job");
+        hfx_scf_options o{};
+        if (opt) o = *opt;
+        const ScfSetup& setup = job_setup(job);
+        Job& j = *job->job;
+        double fock_ms = 0.0;
+        GBuilder g = [&](const double* P, double* G, bool) {
+            j.fock_rhf(P, G);
+            fock_ms += j.stats.ms;
+        };
+        ScfOutput out = rhf_diis(j.basis(), setup, o, P0, g);
+        fill_result(out, res, fock_ms);
+        int K = out.K;
+        if (density) std::memcpy(density, out.P.data(), sizeof(double) * K * K);
+        if (coefficient && !out.C.empty()) std::memcpy(coefficient, out.C.data(), sizeof(double) * K * K);
+        if (mo_energy && !out.e.empty()) std::memcpy(mo_energy, out.e.data(), sizeof(double) * K);
+        if (!out.converged) throw Error(HFX_ERR_NOT_CONVERGED, "SCF did not converge within max_iterations");
+    });
+}
+
+hfx_status hfx_job_uhf(hfx_job* job, const hfx_scf_options* opt, int n_alpha, int n_beta, const double* Pa0,
+                       const double* Pb0, hfx_scf_result* res, double* Pa, double* Pb)
+{
+    return guarded([&] {
+        if (!job) throw Error(HFX_ERR_INVALID, "null job");
+        hfx_scf_options o{};
+        if (opt) o = *opt;
+        const ScfSetup& setup = job_setup(job);
+        Job& j = *job->job;
+        double fock_ms = 0.0;
+        JKBuilder jk = [&](const double* a, const double* b, double* J, double* Ka, double* Kb, bool) {
+            j.fock_uhf(a, b, J, Ka, Kb);
+            fock_ms += j.stats.ms;
+        };
+        ScfOutput out = uhf_diis(j.basis(), setup, o, n_alpha, n_beta, Pa0, Pb0, jk);
+        fill_result(out, res, fock_ms);
+        int K = out.K;
+        if (Pa) std::memcpy(Pa, out.P.data(), sizeof(double) * K * K);
+        if (Pb) std::memcpy(Pb, out.P2.data(), sizeof(double) * K * K);
         if (!out.converged) throw Error(HFX_ERR_NOT_CONVERGED, "SCF did not converge within max_iterations");
     });
 }

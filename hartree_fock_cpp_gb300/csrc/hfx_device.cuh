@@ -4,7 +4,7 @@
 // HBM layout of one job (all arrays device-resident for the job's lifetime):
 //   DPair[npairs]    one record per shell pair (A >= B in shell order), the
 //                    shell with the higher L stored first ("0" side)
-//   pp_geo[npp]      double4 per primitive pair: (p, Px, Py, Pz)
+//   pp_geo[npp]      PairGeo per primitive pair: (p, Px, Py, Pz)
 //   E pool           per primitive pair, the dense Hermite->Cartesian matrix
 //                    E[ab][tuv] (n0*n1 x H(l0+l1)), with the primitive weights
 //                    w_i(a) w_j(b) (coefficient x cart_norm) and
@@ -23,6 +23,20 @@ constexpr int kBoysM = 20;          // orders stored (12 + 7 Taylor terms + 1)
 constexpr int kBoysInvStep = 16;    // grid step 1/16
 constexpr int kBoysTMax = 36;       // table covers [0, 36]; upward recursion beyond
 constexpr int kBoysN = kBoysTMax * kBoysInvStep + 1;
+
+// Primitive-pair geometry: p = alpha + beta and the product centre P.
+struct __align__(32) PairGeo {
+    double p, x, y, z;
+};
+__host__ __device__ inline PairGeo make_pairgeo(double p, double x, double y, double z)
+{
+    PairGeo g;
+    g.p = p;
+    g.x = x;
+    g.y = y;
+    g.z = z;
+    return g;
+}
 
 struct __align__(16) DPair {
     int bf0, bf1;    // first basis function of shell 0 / shell 1
@@ -57,7 +71,7 @@ struct Task {
 // Work-list descriptor of one launch.
 struct LaunchArgs {
     const DPair* pairs;
-    const double4* pp_geo;
+    const PairGeo* pp_geo;
     const double* epool;
     const float4* pp_geo32;
     const float* epool32;

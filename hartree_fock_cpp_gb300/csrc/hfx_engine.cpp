@@ -55,6 +55,8 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
     cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
     cuda_check(cudaEventCreate(&ev0_), "event");
     cuda_check(cudaEventCreate(&ev1_), "event");
+    cuda_check(cudaEventCreate(&evk0_), "event");
+    cuda_check(cudaEventCreate(&evk1_), "event");
     d_counter_.alloc(4);
 
     // Boys table F_m(k/16), m < kBoysM
@@ -66,7 +68,7 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
     build_pairs();
     compute_schwarz();
     std::vector<Task> tasks;
-    build_tasks(opt_.screening_threshold, tasks, maxacc_, maxw_, maxr_);
+    build_tasks(opt_.screening_threshold, tasks, maxacc_, maxw_, maxr_, &flops_, &prim_quartets_);
     ntasks_ = (int)tasks.size();
     d_tasks_.upload(tasks, stream_);
     cuda_check(cudaStreamSynchronize(stream_), "job setup");
@@ -78,6 +80,8 @@ Job::~Job()
     if (stream_) cudaStreamSynchronize(stream_);
     if (ev0_) cudaEventDestroy(ev0_);
     if (ev1_) cudaEventDestroy(ev1_);
+    if (evk0_) cudaEventDestroy(evk0_);
+    if (evk1_) cudaEventDestroy(evk1_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -111,7 +115,7 @@ PairData build_pair_data(const Basis& basis)
                     hermite_1d(l0, l1, a, be, S0.x, S1.x, Ex);
                     hermite_1d(l0, l1, a, be, S0.y, S1.y, Ey);
                     hermite_1d(l0, l1, a, be, S0.z, S1.z, Ez);
-                    pd.geo.push_back(make_double4(p, (a * S0.x + be * S1.x) / p, (a * S0.y + be * S1.y) / p,
+                    pd.geo.push_back(make_pairgeo(p, (a * S0.x + be * S1.x) / p, (a * S0.y + be * S1.y) / p,
                                                   (a * S0.z + be * S1.z) / p));
                     size_t base = pd.epool.size();
                     pd.epool.resize(base + (size_t)n0 * n1 * H, 0.0);
@@ -230,7 +234,8 @@ void Job::compute_schwarz()
 
 void Job::schwarz_host(std::vector<double>& Q) const { Q = qbf_; }
 
-void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr) const
+void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops,
+                      double* prims) const
 {
     int np = (int)hpairs_.size();
     // order pairs so that the pair with the larger (L, l0) is the bra
@@ -246,22 +251,42 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
             tasks.push_back({bra, ket});
         }
     std::vector<double> c(tasks.size());
+    double fsum = 0.0, psum = 0.0;
     for (size_t t = 0; t < tasks.size(); ++t) {
         const HostPair& b = hpairs_[tasks[t].bra];
         const HostPair& k = hpairs_[tasks[t].ket];
         c[t] = (double)b.npp * k.npp * flops_per_prim(b.l0, b.l1, k.l0, k.l1);
+        fsum += c[t];
+        psum += (double)b.npp * k.npp;
         int L1 = b.l0 + b.l1, L2 = k.l0 + k.l1;
         int nab = ncart(b.l0) * ncart(b.l1), ncd = ncart(k.l0) * ncart(k.l1);
         maxacc = std::max(maxacc, nab * ncd);
         maxw = std::max(maxw, nherm(L1) * ncd);
         maxr = std::max(maxr, nherm(L1 + L2));
     }
+    if (flops) *flops = fsum;
+    if (prims) *prims = psum;
     std::vector<size_t> idx(tasks.size());
     std::iota(idx.begin(), idx.end(), 0);
     std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return c[x] > c[y]; });
     std::vector<Task> sorted(tasks.size());
     for (size_t t = 0; t < idx.size(); ++t) sorted[t] = tasks[idx[t]];
     tasks.swap(sorted);
+}
+
+void Job::record_stats(int launches)
+{
+    float ms = 0.f, kms = 0.f;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    cudaEventElapsedTime(&kms, evk0_, evk1_);
+    stats.ms = ms;
+    stats.kernel_ms = kms;
+    stats.quartets = ntasks_;
+    stats.quartets_fp32 = 0;
+    stats.prim_quartets = prim_quartets_;
+    stats.flops_fp64 = flops_;
+    stats.flops_fp32 = 0;
+    stats.launches = launches;
 }
 
 void Job::fock_rhf_device(const double* dP, double* dG)
@@ -279,15 +304,13 @@ void Job::fock_rhf_device(const double* dP, double* dG)
     a.Jacc = d_J_.p;
     a.Kacc = d_K_.p;
     cuda_check(cudaEventRecord(ev0_, stream_), "event");
+    cuda_check(cudaEventRecord(evk0_, stream_), "event");
     run_tasks(MODE_JK, 1, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ev0_, ev1_);
-    stats.ms = ms;
-    stats.quartets = ntasks_;
-    stats.launches = 2;
+    record_stats(2);
 }
 
 void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb)
@@ -311,15 +334,13 @@ void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, doub
     a.Jacc = d_J_.p;
     a.Kacc = d_K_.p;
     a.Kacc2 = d_K2_.p;
+    cuda_check(cudaEventRecord(evk0_, stream_), "event");
     run_tasks(MODE_JK, 2, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_uhf(d_J_.p, d_K_.p, d_K2_.p, dJ, dKa, dKb, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ev0_, ev1_);
-    stats.ms = ms;
-    stats.quartets = ntasks_;
-    stats.launches = 3;
+    record_stats(3);
 }
 
 void Job::fock_rhf(const double* P, double* G)

@@ -70,7 +70,7 @@ struct HostPair {
 struct PairData {
     std::vector<HostPair> hpairs;
     std::vector<DPair> dpairs;
-    std::vector<double4> geo;
+    std::vector<PairGeo> geo;
     std::vector<double> epool;
 };
 PairData build_pair_data(const Basis& b);
@@ -97,23 +97,25 @@ public:
 private:
     void build_pairs();
     void compute_schwarz();
-    void build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr) const;
+    void build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops = nullptr,
+                     double* prims = nullptr) const;
     void run_tasks(int mode, int nk, const std::vector<Task>* host_tasks, const DevBuf<Task>& tasks, int ntasks,
                    int maxacc, int maxw, int maxr, LaunchArgs a);
     LaunchArgs base_args() const;
+    void record_stats(int launches);
 
     Basis basis_;
     hfx_options opt_;
     int device_ = 0;
     int nsm_ = 1;
     cudaStream_t stream_ = nullptr;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evk0_ = nullptr, evk1_ = nullptr;
 
     std::vector<HostPair> hpairs_;
     std::vector<double> qsh_;     // per pair
     std::vector<double> qbf_;     // per BF pair
     DevBuf<DPair> d_pairs_;
-    DevBuf<double4> d_ppgeo_;
+    DevBuf<PairGeo> d_ppgeo_;
     DevBuf<double> d_epool_;
     DevBuf<double> d_boys_;
     DevBuf<double> d_qbf_;

@@ -169,13 +169,13 @@ __global__ void __launch_bounds__(128) k_quartet_generic(LaunchArgs a, int maxac
         for (int e = tid; e < nout; e += blockDim.x) acc[e] = 0.0;
 
         for (int ij = 0; ij < bra.npp; ++ij) {
-            const double4 g1 = a.pp_geo[bra.pp0 + ij];
+            const PairGeo g1 = a.pp_geo[bra.pp0 + ij];
             const double* Eij = epool + bra.e_off + (long long)ij * nab * H1;
             for (int kl = 0; kl < ket.npp; ++kl) {
-                const double4 g2 = a.pp_geo[ket.pp0 + kl];
+                const PairGeo g2 = a.pp_geo[ket.pp0 + kl];
                 const double* Ekl = epool + ket.e_off + (long long)kl * ncd * H2;
                 if (warp == 0)
-                    hermite_R_warp(g1.x, g1.y, g1.z, g1.w, g2.x, g2.y, g2.z, g2.w, L, Ra, Rb, seeds, idx3, comp,
+                    hermite_R_warp(g1.p, g1.x, g1.y, g1.z, g2.p, g2.x, g2.y, g2.z, L, Ra, Rb, seeds, idx3, comp,
                                    a.boys);
                 __syncthreads();
                 const double* R = (L % 2 == 0) ? Ra : Rb;

@@ -165,6 +165,8 @@ void solve_full_piv(int n, const double* Ain, const double* b, double* x)
     std::vector<int> colp(n);
     std::iota(colp.begin(), colp.end(), 0);
     int rank = n;
+    double maxpiv = 0.0;
+    const double thr = 2.220446049250313e-16 * n;  // Eigen FullPivLU default threshold
     for (int k = 0; k < n; ++k) {
         int pi = k, pj = k;
         double best = -1.0;
@@ -175,7 +177,8 @@ void solve_full_piv(int n, const double* Ain, const double* b, double* x)
                     pi = i;
                     pj = j;
                 }
-        if (best <= 0.0) {
+        if (k == 0) maxpiv = best;
+        if (best <= 0.0 || best <= thr * maxpiv) {
             rank = k;
             break;
         }

@@ -138,7 +138,33 @@ static bool finite_all(const std::vector<double>& v)
     return true;
 }
 
-ScfOutput rhf_diis(const Basis& b, const hfx_scf_options& opt_in, const double* P0, const GBuilder& gbuild)
+ScfSetup scf_setup(const Basis& b)
+{
+    ScfSetup s;
+    int K = b.K;
+    s.K = K;
+    std::vector<double> T, V;
+    one_electron(b, s.S, T, V);
+    s.H.resize((size_t)K * K);
+    for (int i = 0; i < K * K; ++i) s.H[i] = T[i] + V[i];
+    s.E_nuc = nuclear_repulsion(b);
+    s.X = xmatrix(K, s.S);
+    return s;
+}
+
+ScfOutput rhf_diis(const Basis& b, const hfx_scf_options& opt, const double* P0, const GBuilder& g)
+{
+    return rhf_diis(b, scf_setup(b), opt, P0, g);
+}
+
+ScfOutput uhf_diis(const Basis& b, const hfx_scf_options& opt, int na, int nb, const double* Pa0, const double* Pb0,
+                   const JKBuilder& jk)
+{
+    return uhf_diis(b, scf_setup(b), opt, na, nb, Pa0, Pb0, jk);
+}
+
+ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt_in, const double* P0,
+                   const GBuilder& gbuild)
 {
     auto t0 = std::chrono::steady_clock::now();
     hfx_scf_options opt = opt_in;
@@ -146,12 +172,10 @@ ScfOutput rhf_diis(const Basis& b, const hfx_scf_options& opt_in, const double* 
     int K = b.K;
     int n_e = -opt.charge;
     for (int z : b.atom_Z) n_e += z;
-    std::vector<double> S, T, V;
-    one_electron(b, S, T, V);
-    std::vector<double> H(K * K);
-    for (int i = 0; i < K * K; ++i) H[i] = T[i] + V[i];
-    double E_nuc = nuclear_repulsion(b);
-    std::vector<double> X = xmatrix(K, S);
+    const std::vector<double>& S = setup.S;
+    const std::vector<double>& H = setup.H;
+    const std::vector<double>& X = setup.X;
+    double E_nuc = setup.E_nuc;
     std::vector<double> P(K * K, 0.0);
     if (P0) P.assign(P0, P0 + K * K);
     std::deque<std::vector<double>> fh, eh;
@@ -218,8 +242,8 @@ ScfOutput rhf_diis(const Basis& b, const hfx_scf_options& opt_in, const double* 
     return out;
 }
 
-ScfOutput uhf_diis(const Basis& b, const hfx_scf_options& opt_in, int na, int nb, const double* Pa0,
-                   const double* Pb0, const JKBuilder& jk)
+ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt_in, int na, int nb,
+                   const double* Pa0, const double* Pb0, const JKBuilder& jk)
 {
     auto t0 = std::chrono::steady_clock::now();
     hfx_scf_options opt = opt_in;
@@ -228,12 +252,10 @@ ScfOutput uhf_diis(const Basis& b, const hfx_scf_options& opt_in, int na, int nb
     int n_e = -opt.charge;
     for (int z : b.atom_Z) n_e += z;
     if (n_e != na + nb) throw Error(HFX_ERR_INVALID, "inconsistency in electron number");
-    std::vector<double> S, T, V;
-    one_electron(b, S, T, V);
-    std::vector<double> H(K * K);
-    for (int i = 0; i < K * K; ++i) H[i] = T[i] + V[i];
-    double E_nuc = nuclear_repulsion(b);
-    std::vector<double> X = xmatrix(K, S);
+    const std::vector<double>& S = setup.S;
+    const std::vector<double>& H = setup.H;
+    const std::vector<double>& X = setup.X;
+    double E_nuc = setup.E_nuc;
     std::vector<double> Pa(K * K, 0.0), Pb(K * K, 0.0);
     if (Pa0) Pa.assign(Pa0, Pa0 + K * K);
     if (Pb0) Pb.assign(Pb0, Pb0 + K * K);

@@ -23,6 +23,20 @@ struct ScfOutput {
     std::vector<double> P, P2, C, e, e2;
 };
 
+// Per-molecule setup of the SCF (S, H = T + V, X = S^-1/2, E_nuc), computed
+// once and reusable across SCFs of the same geometry.
+struct ScfSetup {
+    int K = 0;
+    std::vector<double> S, H, X;
+    double E_nuc = 0.0;
+};
+ScfSetup scf_setup(const Basis& b);
+
+ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt, const double* P0,
+                   const GBuilder& g);
+ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt, int na, int nb,
+                   const double* Pa0, const double* Pb0, const JKBuilder& jk);
+
 ScfOutput rhf_diis(const Basis& b, const hfx_scf_options& opt, const double* P0, const GBuilder& g);
 ScfOutput uhf_diis(const Basis& b, const hfx_scf_options& opt, int na, int nb, const double* Pa0, const double* Pb0,
                    const JKBuilder& jk);

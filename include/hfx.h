@@ -138,7 +138,8 @@ hfx_status hfx_eri_gpu(const hfx_functions *basis, double threshold, double *out
 
 /* Statistics of the last Fock build. */
 typedef struct {
-    double ms;                /* device time of the build (CUDA events) */
+    double ms;                /* device time of the whole build (CUDA events) */
+    double kernel_ms;         /* device time of the shell-quartet kernel launches alone */
     double quartets;          /* surviving shell quartets */
     double quartets_fp32;     /* of which computed in FP32 */
     double prim_quartets;     /* primitive quartets evaluated */
@@ -189,6 +190,15 @@ hfx_status hfx_rhf_diis(const hfx_molecule *mol, const hfx_scf_options *opt, con
 hfx_status hfx_uhf_diis(const hfx_molecule *mol, const hfx_scf_options *opt, int n_alpha, int n_beta,
                         const double *Pa0, const double *Pb0, hfx_scf_result *res, double *Pa, double *Pb,
                         double *mo_energy_a, double *mo_energy_b);
+
+/* RHF / UHF SCF on an existing job (its basis, pair data and Schwarz table
+ * stay resident; S, H and S^-1/2 are computed once per job).  Same semantics
+ * and outputs as hfx_rhf_diis / hfx_uhf_diis; the job's screening and
+ * precision options apply, the molecule's charge comes from opt. */
+hfx_status hfx_job_rhf(hfx_job *job, const hfx_scf_options *opt, const double *P0, hfx_scf_result *res,
+                       double *density, double *coefficient, double *mo_energy);
+hfx_status hfx_job_uhf(hfx_job *job, const hfx_scf_options *opt, int n_alpha, int n_beta, const double *Pa0,
+                       const double *Pb0, hfx_scf_result *res, double *Pa, double *Pb);
 
 /* The same drivers with a caller-supplied two-electron builder in place of
  * the GPU engine: the host SCF loop (DIIS, eigensolver, convergence logic)

@@ -13,8 +13,9 @@ Contents
     integrals.hpp compiled unchanged; only where a reference checkout exists);
   * a numpy restatement of the reference's SCF drivers rhf_diis
     (include/scf.hpp:205-419) and uhf_diis (include/scf.hpp:423-682), with
-    numpy.linalg.eigh standing in for Eigen's SelfAdjointEigenSolver and
-    numpy.linalg.solve for fullPivLu (Eigen is not available here).
+    numpy.linalg.eigh standing in for Eigen's SelfAdjointEigenSolver and a
+    complete-pivoting LU solve restating Eigen's fullPivLu rank handling
+    (Eigen is not available here).
 """
 import csv
 import ctypes
@@ -295,8 +296,51 @@ def fock_diis(fock_hist, err_hist):         # linalg.hpp:405-510
     B[n, :n] = 1.0
     rhs = np.zeros(n + 1)
     rhs[n] = 1.0
-    c = np.linalg.lstsq(B, rhs, rcond=None)[0] if np.linalg.cond(B) > 1e15 else np.linalg.solve(B, rhs)
+    c = full_piv_lu_solve(B, rhs)
     return sum(c[i] * fock_hist[i] for i in range(n))
+
+
+def full_piv_lu_solve(A, b):
+    """Gaussian elimination with complete pivoting, rank decided like Eigen's
+    FullPivLU (pivots below eps*min(rows,cols)*|largest pivot| count as zero;
+    the free unknowns of a rank-deficient system are set to zero) -- the
+    reference's diis_coefficients uses A.fullPivLu().solve(rhs)
+    (linalg.hpp:430-447)."""
+    A = np.array(A, dtype=np.float64)
+    r = np.array(b, dtype=np.float64)
+    n = A.shape[0]
+    colp = list(range(n))
+    maxpiv = 0.0
+    rank = n
+    for k in range(n):
+        sub = np.abs(A[k:, k:])
+        pi, pj = np.unravel_index(np.argmax(sub), sub.shape)
+        pi += k
+        pj += k
+        piv = abs(A[pi, pj])
+        if k == 0:
+            maxpiv = piv
+        if piv <= np.finfo(float).eps * n * maxpiv or piv == 0.0:
+            rank = k
+            break
+        if pi != k:
+            A[[pi, k], :] = A[[k, pi], :]
+            r[[pi, k]] = r[[k, pi]]
+        if pj != k:
+            A[:, [pj, k]] = A[:, [k, pj]]
+            colp[pj], colp[k] = colp[k], colp[pj]
+        for i in range(k + 1, n):
+            f = A[i, k] / A[k, k]
+            if f != 0.0:
+                A[i, k:] -= f * A[k, k:]
+                r[i] -= f * r[k]
+    y = np.zeros(n)
+    for i in range(rank - 1, -1, -1):
+        y[i] = (r[i] - A[i, i + 1:rank] @ y[i + 1:rank]) / A[i, i]
+    x = np.zeros(n)
+    for j in range(n):
+        x[colp[j]] = y[j]
+    return x
 
 
 def _energy(P, F, H):                       # scf.hpp:28-39
