@@ -159,7 +159,7 @@ def run_reference(args):
     vals = []
     base = None
     for s in range(args.warmup + args.steps):
-        b = cpu_baseline(cfg, "cc-pVDZ", iters, sample_quartets=max(400, 100 * nthreads), nthreads=nthreads,
+        b = cpu_baseline(cfg, "cc-pVDZ", iters, sample_quartets=2000 * nthreads, nthreads=nthreads,
                          seed=20261203 + s)
         if s >= args.warmup:
             vals.append(b["seconds_per_solve"])
@@ -289,7 +289,7 @@ def run_engine(args):
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        b = cpu_baseline(cfg, basis, iters, sample_quartets=max(400, 100 * nthreads), nthreads=nthreads)
+        b = cpu_baseline(cfg, basis, iters, sample_quartets=2000 * nthreads, nthreads=nthreads)
         cpu = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
