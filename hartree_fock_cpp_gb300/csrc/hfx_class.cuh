@@ -1,0 +1,312 @@
+// hfx_class.cuh -- thread-per-shell-quartet kernels for the small
+// angular-momentum classes (at most 36 Cartesian integrals per shell quartet
+// and total L <= 4: (ss|ss) (ps|ss) (ps|ps) (pp|ss) (pp|ps) (ds|ss) (ds|ps)
+// (ds|ds) (dp|ss) (dd|ss)), instantiated for T = double and T = float.
+//
+// These classes carry most of the primitive quartets of contracted basis sets
+// (cc-pVDZ carbon s shells have 9 primitives, so one (ss|ss) shell quartet is
+// up to 6561 primitive quartets).  One thread owns one shell quartet and loops
+// over all of its primitive quartets with every index, loop bound and
+// sparsity pattern fixed at compile time: the Boys seeds, the R_{tuv} table,
+// the ket-transformed W and the Cartesian accumulators stay in registers; no
+// shared memory, no barriers.  The quartet list of a class is sorted by
+// primitive count, so a warp's 32 lanes run loops of equal length.
+//
+// Per primitive quartet (the reference's primitive_repulsion,
+// integrals.hpp:624-699, evaluated once per shell quartet here):
+//   s_m = 2 pi^{5/2} / (p q sqrt(p+q)) (-2 rho)^m F_m(T)
+//   R   in-place downward recursion over m (integrals.hpp:541-618)
+//   W_cd[tuv] = sum_{tnp in nz(cd)} (-1)^{|tnp|} c^{kl}_{cd,tnp} R[tuv+tnp]
+//   acc[ab][cd] += sum_{tuv in nz(ab)} c^{ij}_{ab,tuv} W_cd[tuv]
+// with the coefficient records of hfx_device.cuh.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "hfx_device.cuh"
+
+namespace hfx {
+
+__host__ __device__ constexpr int c_nc(int l) { return (l + 1) * (l + 2) / 2; }
+__host__ __device__ constexpr int c_nh(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
+
+__host__ __device__ constexpr int comp_x(int L, int c)
+{
+    int n = 0;
+    for (int a = 0; a <= L; ++a)
+        for (int b = 0; b <= L - a; ++b) {
+            if (n == c) return a;
+            ++n;
+        }
+    return 0;
+}
+__host__ __device__ constexpr int comp_y(int L, int c)
+{
+    int n = 0;
+    for (int a = 0; a <= L; ++a)
+        for (int b = 0; b <= L - a; ++b) {
+            if (n == c) return b;
+            ++n;
+        }
+    return 0;
+}
+__host__ __device__ constexpr int comp_z(int L, int c) { return L - comp_x(L, c) - comp_y(L, c); }
+
+__host__ __device__ constexpr int hidx(int t, int u, int v)
+{
+    return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 + t * (t + u + v + 1) - t * (t - 1) / 2 + u;
+}
+
+// number of non-zero coefficients of component pair ab of a (la, lb) pair
+__host__ __device__ constexpr int n_coef_ab(int la, int lb, int ab)
+{
+    int nb = c_nc(lb);
+    int a = ab / nb, b = ab % nb;
+    return (comp_x(la, a) + comp_x(lb, b) + 1) * (comp_y(la, a) + comp_y(lb, b) + 1) *
+           (comp_z(la, a) + comp_z(lb, b) + 1);
+}
+__host__ __device__ constexpr int coef_off(int la, int lb, int ab)
+{
+    int o = 0;
+    for (int x = 0; x < ab; ++x) o += n_coef_ab(la, lb, x);
+    return o;
+}
+__host__ __device__ constexpr int n_coef(int la, int lb) { return coef_off(la, lb, c_nc(la) * c_nc(lb)); }
+__host__ __device__ constexpr int rec_stride(int la, int lb) { return (4 + n_coef(la, lb) + 1) & ~1; }
+
+
+// F_0..F_L: table + Taylor for F_L and exp(-T), downward recursion; beyond
+// the table the asymptotic F_0 and upward recursion.
+template <typename T, int L>
+__device__ __forceinline__ void boys_all(T Tv, const T* __restrict__ tab, T (&F)[L + 1])
+{
+    if (Tv < (T)kBoysTMax) {
+        const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
+        const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+        const T* f = tab + k * kBoysM + L;
+        T r;
+        if constexpr (sizeof(T) == 8) {
+            r = __ldg(f + 6) * (T)(1.0 / 720.0);
+            r = fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
+            r = fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
+        } else {
+            r = __ldg(f + 4) * (T)(1.0 / 24.0);
+        }
+        r = fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
+        r = fma(r, nd, __ldg(f + 2) * (T)0.5);
+        r = fma(r, nd, __ldg(f + 1));
+        F[L] = fma(r, nd, __ldg(f));
+        if constexpr (L > 0) {
+            T x;
+            if constexpr (sizeof(T) == 8) {
+                x = (T)(1.0 / 5040.0);
+                x = fma(x, nd, (T)(1.0 / 720.0));
+                x = fma(x, nd, (T)(1.0 / 120.0));
+                x = fma(x, nd, (T)(1.0 / 24.0));
+            } else {
+                x = (T)(1.0 / 24.0);
+            }
+            x = fma(x, nd, (T)(1.0 / 6.0));
+            x = fma(x, nd, (T)0.5);
+            x = fma(x, nd, (T)1);
+            x = fma(x, nd, (T)1);
+            const T e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+            const T t2 = Tv + Tv;
+#pragma unroll
+            for (int m = L - 1; m >= 0; --m) F[m] = fma(t2, F[m + 1], e) * ((T)1 / (T)(2 * m + 1));
+        }
+    } else {
+        const T rs = rsqrt(Tv);
+        F[0] = (T)0.88622692545275801365 * rs;
+        if constexpr (L > 0) {
+            const T inv2T = (T)0.5 * rs * rs;
+#pragma unroll
+            for (int m = 0; m < L; ++m) F[m + 1] = (T)(2 * m + 1) * F[m] * inv2T;
+        }
+    }
+}
+
+template <typename T, int L>
+__device__ __forceinline__ void hermite_R(T X, T Y, T Z, const T (&s)[L + 1], T (&R)[c_nh(L)])
+{
+    R[0] = s[L];
+#pragma unroll
+    for (int n = L - 1; n >= 0; --n) {
+#pragma unroll
+        for (int sl = L - n; sl >= 1; --sl) {
+#pragma unroll
+            for (int t = 0; t <= sl; ++t) {
+#pragma unroll
+                for (int u = 0; u <= sl - t; ++u) {
+                    const int v = sl - t - u;
+                    T val;
+                    if (t > 0) {
+                        val = X * R[hidx(t - 1, u, v)];
+                        if (t > 1) val = fma((T)(t - 1), R[hidx(t - 2, u, v)], val);
+                    } else if (u > 0) {
+                        val = Y * R[hidx(t, u - 1, v)];
+                        if (u > 1) val = fma((T)(u - 1), R[hidx(t, u - 2, v)], val);
+                    } else {
+                        val = Z * R[hidx(t, u, v - 1)];
+                        if (v > 1) val = fma((T)(v - 1), R[hidx(t, u, v - 2)], val);
+                    }
+                    R[hidx(t, u, v)] = val;
+                }
+            }
+        }
+        R[0] = s[n];
+    }
+}
+
+__device__ __forceinline__ long long spidx(int a, int b)
+{
+    int hi = a > b ? a : b, lo = a > b ? b : a;
+    return (long long)hi * (hi + 1) / 2 + lo;
+}
+
+template <typename T, int LA, int LB, int LC, int LD, int NK>
+__global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
+{
+    constexpr int L1 = LA + LB, L2 = LC + LD, L = L1 + L2;
+    constexpr int NB = c_nc(LB), ND = c_nc(LD);
+    constexpr int NAB = c_nc(LA) * NB, NCD = c_nc(LC) * ND;
+    constexpr int H1 = c_nh(L1), HL = c_nh(L);
+    constexpr int SB = rec_stride(LA, LB), SK = rec_stride(LC, LD);
+
+    const int task = blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= a.ntasks) return;
+    const Task tk = a.tasks[task];
+    const DPair bra = a.pairs[tk.bra];
+    const DPair ket = a.pairs[tk.ket];
+
+    T acc[NAB][NCD];
+#pragma unroll
+    for (int x = 0; x < NAB; ++x)
+#pragma unroll
+        for (int y = 0; y < NCD; ++y) acc[x][y] = (T)0;
+
+    const T* __restrict__ recb = a.rec + bra.rec_off;
+    const T* __restrict__ reck = a.rec + ket.rec_off;
+    for (int ij = 0; ij < bra.npp; ++ij) {
+        const T* rb = recb + ij * SB;
+        const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
+        const T* cb = rb + 4;
+        for (int kl = 0; kl < ket.npp; ++kl) {
+            const T* rk = reck + kl * SK;
+            const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
+            const T* ck = rk + 4;
+            const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+            const T pq = p + q;
+            const T rho = p * q / pq;
+            const T Tv = rho * (X * X + Y * Y + Z * Z);
+            const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
+            T F[L + 1];
+            boys_all<T, L>(Tv, a.boys, F);
+            T sd[L + 1];
+            {
+                const T m2r = (T)-2 * rho;
+                T pw = pref;
+#pragma unroll
+                for (int m = 0; m <= L; ++m) {
+                    sd[m] = pw * F[m];
+                    pw *= m2r;
+                }
+            }
+            T R[HL];
+            hermite_R<T, L>(X, Y, Z, sd, R);
+#pragma unroll
+            for (int cd = 0; cd < NCD; ++cd) {
+                const int c = cd / ND, d = cd % ND;
+                const int nx = comp_x(LC, c) + comp_x(LD, d), ny = comp_y(LC, c) + comp_y(LD, d),
+                          nz = comp_z(LC, c) + comp_z(LD, d);
+                T W[H1];
+#pragma unroll
+                for (int h = 0; h < H1; ++h) W[h] = (T)0;
+                int k = coef_off(LC, LD, cd);
+#pragma unroll
+                for (int tn = 0; tn <= nx; ++tn)
+#pragma unroll
+                    for (int nu = 0; nu <= ny; ++nu)
+#pragma unroll
+                        for (int ph = 0; ph <= nz; ++ph, ++k) {
+                            T e = __ldg(ck + k);
+                            if ((tn + nu + ph) & 1) e = -e;
+#pragma unroll
+                            for (int s1 = 0; s1 <= L1; ++s1)
+#pragma unroll
+                                for (int t = 0; t <= s1; ++t)
+#pragma unroll
+                                    for (int u = 0; u <= s1 - t; ++u) {
+                                        const int v = s1 - t - u;
+                                        W[hidx(t, u, v)] = fma(e, R[hidx(t + tn, u + nu, v + ph)], W[hidx(t, u, v)]);
+                                    }
+                        }
+#pragma unroll
+                for (int ab = 0; ab < NAB; ++ab) {
+                    const int aa = ab / NB, bb = ab % NB;
+                    const int mx = comp_x(LA, aa) + comp_x(LB, bb), my = comp_y(LA, aa) + comp_y(LB, bb),
+                              mz = comp_z(LA, aa) + comp_z(LB, bb);
+                    int kb = coef_off(LA, LB, ab);
+                    T s = acc[ab][cd];
+#pragma unroll
+                    for (int t = 0; t <= mx; ++t)
+#pragma unroll
+                        for (int u = 0; u <= my; ++u)
+#pragma unroll
+                            for (int v = 0; v <= mz; ++v, ++kb) s = fma(__ldg(cb + kb), W[hidx(t, u, v)], s);
+                    acc[ab][cd] = s;
+                }
+            }
+        }
+    }
+
+    // digestion (FP64)
+    const int K = a.K;
+    const bool same_pair = (tk.bra == tk.ket);
+#pragma unroll
+    for (int ab = 0; ab < NAB; ++ab) {
+        const int ia = ab / NB, ib = ab % NB;
+        const int i = bra.bf0 + ia, j = bra.bf1 + ib;
+        const long long pij = spidx(i, j);
+        const double qb = __ldg(a.Qbf + pij);
+        if (bra.same && ia < ib) continue;
+#pragma unroll
+        for (int cd = 0; cd < NCD; ++cd) {
+            const int ic = cd / ND, id = cd % ND;
+            const int k = ket.bf0 + ic, l = ket.bf1 + id;
+            if (ket.same && ic < id) continue;
+            const long long pkl = spidx(k, l);
+            if (same_pair && pij < pkl) continue;
+            if (a.thr >= 0.0 && qb * __ldg(a.Qbf + pkl) < a.thr) continue;
+            const double v =
+                (double)acc[ab][cd] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
+            atomicAdd(a.J + (long long)i * K + j, __ldg(a.Dj + (long long)k * K + l) * v);
+            atomicAdd(a.J + (long long)k * K + l, __ldg(a.Dj + (long long)i * K + j) * v);
+            atomicAdd(a.Kx + (long long)i * K + k, __ldg(a.Dk + (long long)j * K + l) * v);
+            atomicAdd(a.Kx + (long long)j * K + l, __ldg(a.Dk + (long long)i * K + k) * v);
+            atomicAdd(a.Kx + (long long)i * K + l, __ldg(a.Dk + (long long)j * K + k) * v);
+            atomicAdd(a.Kx + (long long)j * K + k, __ldg(a.Dk + (long long)i * K + l) * v);
+            if constexpr (NK == 2) {
+                atomicAdd(a.Kx2 + (long long)i * K + k, __ldg(a.Dk2 + (long long)j * K + l) * v);
+                atomicAdd(a.Kx2 + (long long)j * K + l, __ldg(a.Dk2 + (long long)i * K + k) * v);
+                atomicAdd(a.Kx2 + (long long)i * K + l, __ldg(a.Dk2 + (long long)j * K + k) * v);
+                atomicAdd(a.Kx2 + (long long)j * K + k, __ldg(a.Dk2 + (long long)i * K + l) * v);
+            }
+        }
+    }
+}
+
+template <typename T, int LA, int LB, int LC, int LD>
+cudaError_t launch_small(const SmallArgs<T>& a, int nk, cudaStream_t st)
+{
+    if (a.ntasks == 0) return cudaSuccess;
+    const int block = 128;
+    const int grid = (a.ntasks + block - 1) / block;
+    if (nk == 2)
+        k_small<T, LA, LB, LC, LD, 2><<<grid, block, 0, st>>>(a);
+    else
+        k_small<T, LA, LB, LC, LD, 1><<<grid, block, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace hfx

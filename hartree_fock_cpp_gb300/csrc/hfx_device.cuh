@@ -39,14 +39,32 @@ __host__ __device__ inline PairGeo make_pairgeo(double p, double x, double y, do
 }
 
 struct __align__(16) DPair {
-    int bf0, bf1;    // first basis function of shell 0 / shell 1
-    int l0, l1;      // l0 >= l1
-    int pp0, npp;    // primitive-pair range
-    long long e_off; // offset of the first E block (elements)
-    int same;        // shell 0 == shell 1
-    int id;          // pair id (index in the pair array)
-    double qmax;     // max_ab sqrt((ab|ab)) over the pair's BF pairs
+    int bf0, bf1;      // first basis function of shell 0 / shell 1
+    int l0, l1;        // l0 >= l1
+    int pp0, npp;      // primitive-pair range
+    long long e_off;   // offset of the first dense E block (elements)
+    int same;          // shell 0 == shell 1
+    int id;            // pair id (index in the pair array)
+    double qmax;       // max_ab sqrt((ab|ab)) over the pair's BF pairs
+    long long rec_off; // offset of the first primitive-pair record (elements)
+    int pc;            // pair class l0*(l0+1)/2 + l1
+    int pad;
 };
+
+// Primitive-pair record of the class kernels, for a pair of class (l0, l1):
+//   [p, Px, Py, Pz, c_0 ... c_{ncoef-1}] padded to an even length, where the
+// c_k are the structurally non-zero Hermite->Cartesian coefficients
+//   c = w_i(a) w_j(b) E^x_{ax bx, t} E^y_{ay by, u} E^z_{az bz, v}
+// (weights = contraction coefficient x cart_norm, exp(-mu AB^2) included),
+// ordered by component pair ab (a outer), then t, u, v nested.
+struct PairClassTab {
+    int nab;       // component pairs
+    int ncoef;     // coefficients per record
+    int stride;    // record length (elements)
+    int ab_off;    // offset of this class's ab_start table
+    int k_off;     // offset of this class's per-coefficient tables
+};
+constexpr int kNumPairClasses = 10;   // (00) (10) (11) (20) (21) (22) (30) (31) (32) (33)
 
 __host__ __device__ constexpr int dncart(int l) { return (l + 1) * (l + 2) / 2; }
 __host__ __device__ constexpr int dnherm(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
@@ -95,6 +113,51 @@ struct LaunchArgs {
     // MODE_SCHWARZ
     double* Qout_bf;
     unsigned long long* Qout_sh;
+};
+
+// Arguments of the small-class (thread-per-shell-quartet) kernels.
+template <typename T>
+struct SmallArgs {
+    const DPair* pairs;
+    const T* rec;
+    const Task* tasks;
+    int ntasks;
+    const T* boys;
+    double thr;
+    const double* Qbf;
+    int K;
+    const double* Dj;
+    const double* Dk;
+    const double* Dk2;
+    double* J;
+    double* Kx;
+    double* Kx2;
+};
+
+// Arguments of the warp-per-shell-quartet kernel.
+template <typename T>
+struct WarpArgs {
+    const DPair* pairs;
+    const T* rec;              // primitive-pair records
+    const PairClassTab* pct;   // per pair class
+    const int* ab_start;       // per class: nab+1 offsets into the record coefficients
+    const short* k_herm;       // per coefficient: packed Hermite index of (t,u,v)
+    const short* k_lin;        // per coefficient: t*169+u*13+v, bit 14 = parity of t+u+v
+    const Task* tasks;
+    int ntasks;
+    int* counter;
+    const T* boys;             // [kBoysN][kBoysM], column kBoysM-1 = exp(-T_k)
+    double thr;
+    const double* Qbf;
+    int K;
+    const double* Dj;
+    const double* Dk;
+    const double* Dk2;
+    double* J;
+    double* Kx;
+    double* Kx2;
+    int slice;                 // per-warp shared-memory slice, in T elements
+    int lane_r;                // 1: lane-parallel R allowed for this launch
 };
 
 }  // namespace hfx

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <numeric>
 
 namespace hfx {
@@ -61,16 +62,27 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
 
     // Boys table F_m(k/16), m < kBoysM
     std::vector<double> tab((size_t)kBoysN * kBoysM);
-    for (int k = 0; k < kBoysN; ++k)
-        for (int m = 0; m < kBoysM; ++m) tab[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
+    for (int k = 0; k < kBoysN; ++k) {
+        for (int m = 0; m < kBoysM - 1; ++m) tab[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
+        tab[(size_t)k * kBoysM + kBoysM - 1] = std::exp(-(double)k / kBoysInvStep);
+    }
     d_boys_.upload(tab, stream_);
+    std::vector<float> tab32(tab.begin(), tab.end());
+    d_boys32_.upload(tab32, stream_);
+    for (int s = 0; s < 3; ++s) {
+        cudaStream_t st;
+        cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+        aux_.push_back(st);
+        cudaEvent_t ev;
+        cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+        aux_ev_.push_back(ev);
+    }
+    cuda_check(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming), "event");
 
     build_pairs();
     compute_schwarz();
     std::vector<Task> tasks;
-    build_tasks(opt_.screening_threshold, tasks, maxacc_, maxw_, maxr_, &flops_, &prim_quartets_);
-    ntasks_ = (int)tasks.size();
-    d_tasks_.upload(tasks, stream_);
+    build_jk_groups();
     cuda_check(cudaStreamSynchronize(stream_), "job setup");
 }
 
@@ -82,11 +94,60 @@ Job::~Job()
     if (ev1_) cudaEventDestroy(ev1_);
     if (evk0_) cudaEventDestroy(evk0_);
     if (evk1_) cudaEventDestroy(evk1_);
+    for (auto e : aux_ev_) cudaEventDestroy(e);
+    for (auto st : aux_) cudaStreamDestroy(st);
+    if (fork_ev_) cudaEventDestroy(fork_ev_);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+bool is_small_class(int pcb, int pck)
+{
+    static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0}, {5, 0}};
+    for (auto& c : small)
+        if (c[0] == pcb && c[1] == pck) return true;
+    return false;
+}
+
+static int pair_class(int l0, int l1) { return l0 * (l0 + 1) / 2 + l1; }
+
+const ClassTables& class_tables()
+{
+    static ClassTables ct = [] {
+        ClassTables t;
+        for (int l0 = 0; l0 <= kMaxL; ++l0)
+            for (int l1 = 0; l1 <= l0; ++l1) {
+                PairClassTab pt{};
+                int n0 = ncart(l0), n1 = ncart(l1);
+                pt.nab = n0 * n1;
+                pt.ab_off = (int)t.ab_start.size();
+                pt.k_off = (int)t.k_herm.size();
+                int k = 0;
+                for (int a = 0; a < n0; ++a)
+                    for (int b = 0; b < n1; ++b) {
+                        t.ab_start.push_back(k);
+                        int ax, ay, az, bx, by, bz;
+                        component(l0, a, ax, ay, az);
+                        component(l1, b, bx, by, bz);
+                        for (int tt = 0; tt <= ax + bx; ++tt)
+                            for (int u = 0; u <= ay + by; ++u)
+                                for (int v = 0; v <= az + bz; ++v, ++k) {
+                                    t.k_herm.push_back((short)herm_index(tt, u, v));
+                                    t.k_lin.push_back((short)((tt * 169 + u * 13 + v) | (((tt + u + v) & 1) << 14)));
+                                }
+                    }
+                t.ab_start.push_back(k);
+                pt.ncoef = k;
+                pt.stride = (4 + k + 1) & ~1;
+                t.tab.push_back(pt);
+            }
+        return t;
+    }();
+    return ct;
 }
 
 PairData build_pair_data(const Basis& basis)
 {
+    const ClassTables& ct = class_tables();
     const auto& sh = basis.shells;
     int ns = (int)sh.size();
     PairData pd;
@@ -107,6 +168,9 @@ PairData build_pair_data(const Basis& basis)
             hp.same = (A == B);
             hp.pp0 = (int)pd.geo.size();
             hp.e_off = (long long)pd.epool.size();
+            const int pc = pair_class(l0, l1);
+            const PairClassTab& pt = ct.tab[pc];
+            const long long rec_off = (long long)pd.rec.size();
             int npp = 0;
             int nt = L + 1;
             for (int i = 0; i < S0.nprim(); ++i)
@@ -119,6 +183,13 @@ PairData build_pair_data(const Basis& basis)
                                                   (a * S0.z + be * S1.z) / p));
                     size_t base = pd.epool.size();
                     pd.epool.resize(base + (size_t)n0 * n1 * H, 0.0);
+                    size_t rb = pd.rec.size();
+                    pd.rec.resize(rb + pt.stride, 0.0);
+                    pd.rec[rb] = p;
+                    pd.rec[rb + 1] = (a * S0.x + be * S1.x) / p;
+                    pd.rec[rb + 2] = (a * S0.y + be * S1.y) / p;
+                    pd.rec[rb + 3] = (a * S0.z + be * S1.z) / p;
+                    int kc = 0;
                     for (int c0 = 0; c0 < n0; ++c0) {
                         int ax, ay, az;
                         component(l0, c0, ax, ay, az);
@@ -129,10 +200,13 @@ PairData build_pair_data(const Basis& basis)
                             double* row = pd.epool.data() + base + (size_t)(c0 * n1 + c1) * H;
                             for (int t = 0; t <= ax + bx; ++t)
                                 for (int u = 0; u <= ay + by; ++u)
-                                    for (int v = 0; v <= az + bz; ++v)
-                                        row[herm_index(t, u, v)] = w * Ex[((size_t)ax * (l1 + 1) + bx) * nt + t] *
-                                                                   Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
-                                                                   Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
+                                    for (int v = 0; v <= az + bz; ++v) {
+                                        double c = w * Ex[((size_t)ax * (l1 + 1) + bx) * nt + t] *
+                                                   Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
+                                                   Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
+                                        row[herm_index(t, u, v)] = c;
+                                        pd.rec[rb + 4 + kc++] = c;
+                                    }
                         }
                     }
                     ++npp;
@@ -149,6 +223,8 @@ PairData build_pair_data(const Basis& basis)
             d.same = hp.same ? 1 : 0;
             d.id = (int)pd.hpairs.size();
             d.qmax = 0.0;
+            d.rec_off = rec_off;
+            d.pc = pc;
             pd.dpairs.push_back(d);
             pd.hpairs.push_back(hp);
         }
@@ -162,6 +238,14 @@ void Job::build_pairs()
     d_pairs_.upload(pd.dpairs, stream_);
     d_ppgeo_.upload(pd.geo, stream_);
     d_epool_.upload(pd.epool, stream_);
+    d_rec64_.upload(pd.rec, stream_);
+    std::vector<float> r32(pd.rec.begin(), pd.rec.end());
+    d_rec32_.upload(r32, stream_);
+    const ClassTables& ct = class_tables();
+    d_pct_.upload(ct.tab, stream_);
+    d_abs_.upload(ct.ab_start, stream_);
+    d_kh_.upload(ct.k_herm, stream_);
+    d_kl_.upload(ct.k_lin, stream_);
     cuda_check(cudaStreamSynchronize(stream_), "pair upload");
 }
 
@@ -274,6 +358,164 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     tasks.swap(sorted);
 }
 
+void Job::build_jk_groups()
+{
+    const double thr = opt_.screening_threshold;
+    const bool mixed = opt_.precision == HFX_PREC_MIXED;
+    const double tau = opt_.fp32_threshold;
+    const int np = (int)hpairs_.size();
+    auto pcof = [&](int p) { return pair_class(hpairs_[p].l0, hpairs_[p].l1); };
+    // buckets: small classes per (pcb, pck, fp32); warp classes per (fp32)
+    struct Bucket {
+        std::vector<Task> t;
+        std::vector<double> cost;
+    };
+    std::vector<Bucket> small(2 * 100), warp(2);
+    for (int X = 0; X < np; ++X)
+        for (int Y = 0; Y <= X; ++Y) {
+            const double bound = qsh_[X] * qsh_[Y];
+            if (thr >= 0.0 && bound < thr) continue;
+            int bra = X, ket = Y;
+            if (pcof(Y) > pcof(X)) std::swap(bra, ket);
+            const bool f32 = mixed && bound < tau;
+            const HostPair& b = hpairs_[bra];
+            const HostPair& k = hpairs_[ket];
+            const double c = (double)b.npp * k.npp * flops_per_prim(b.l0, b.l1, k.l0, k.l1);
+            const int pcb = pcof(bra), pck = pcof(ket);
+            Bucket& bk = is_small_class(pcb, pck) ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
+            bk.t.push_back({bra, ket});
+            bk.cost.push_back(c);
+        }
+    std::vector<Task> all;
+    groups_.clear();
+    flops_ = flops32_ = prim_quartets_ = 0.0;
+    quartets32_ = 0.0;
+    ntasks_ = 0;
+    auto sorted = [](Bucket& bk) {
+        std::vector<size_t> idx(bk.t.size());
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return bk.cost[x] > bk.cost[y]; });
+        return idx;
+    };
+    for (int f = 0; f < 2; ++f)
+        for (int pcb = 0; pcb < 10; ++pcb)
+            for (int pck = 0; pck <= pcb; ++pck) {
+                Bucket& bk = small[f * 100 + pcb * 10 + pck];
+                if (bk.t.empty()) continue;
+                LaunchGroup g{};
+                g.kind = 0;
+                g.pcb = pcb;
+                g.pck = pck;
+                g.fp32 = f == 1;
+                g.off = all.size();
+                g.n = bk.t.size();
+                for (size_t i : sorted(bk)) {
+                    all.push_back(bk.t[i]);
+                    g.flops += bk.cost[i];
+                    g.prims += (double)hpairs_[bk.t[i].bra].npp * hpairs_[bk.t[i].ket].npp;
+                }
+                groups_.push_back(g);
+            }
+    const size_t elem[2] = {sizeof(double), sizeof(float)};
+    for (int f = 0; f < 2; ++f) {
+        Bucket& bk = warp[f];
+        if (bk.t.empty()) continue;
+        // tier the warp tasks by the shared-memory slice they need
+        std::vector<size_t> idx = sorted(bk);
+        std::map<int, std::vector<size_t>> tiers;
+        for (size_t i : idx) {
+            const HostPair& b = hpairs_[bk.t[i].bra];
+            const HostPair& k = hpairs_[bk.t[i].ket];
+            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true);
+            int wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - 8064) / (sl * elem[f])));
+            tiers[-wpc].push_back(i);
+        }
+        for (auto& kv : tiers) {
+            LaunchGroup g{};
+            g.kind = 1;
+            g.fp32 = f == 1;
+            g.off = all.size();
+            g.n = kv.second.size();
+            int slice = 0;
+            for (size_t i : kv.second) {
+                const HostPair& b = hpairs_[bk.t[i].bra];
+                const HostPair& k = hpairs_[bk.t[i].ket];
+                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true));
+                all.push_back(bk.t[i]);
+                g.flops += bk.cost[i];
+                g.prims += (double)b.npp * k.npp;
+            }
+            g.slice = (slice + 1) & ~1;
+            g.warps_per_cta = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - 8064) / (g.slice * elem[f])));
+            size_t sm = 8064 + elem[f] * (size_t)g.slice * g.warps_per_cta;
+            int ctas_per_sm = (int)std::max<size_t>(1, (228 * 1024) / (sm + 1024));
+            long long need = ((long long)g.n + g.warps_per_cta - 1) / g.warps_per_cta;
+            g.grid = (int)std::min<long long>(need, (long long)nsm_ * ctas_per_sm);
+            groups_.push_back(g);
+        }
+    }
+    for (const auto& g : groups_) {
+        if (g.fp32) {
+            flops32_ += g.flops;
+            quartets32_ += (double)g.n;
+        } else {
+            flops_ += g.flops;
+        }
+        prim_quartets_ += g.prims;
+    }
+    ntasks_ = (int)all.size();
+    d_jk_tasks_.upload(all, stream_);
+    d_counters_.alloc(std::max<size_t>(1, groups_.size()));
+}
+
+void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
+                    double* Kx2)
+{
+    cuda_check(cudaMemsetAsync(d_counters_.p, 0, sizeof(int) * d_counters_.n, stream_), "memset counters");
+    cuda_check(cudaEventRecord(fork_ev_, stream_), "fork");
+    for (auto st : aux_) cuda_check(cudaStreamWaitEvent(st, fork_ev_, 0), "fork wait");
+    // warp groups (the long ones) on the main stream, small classes spread over the others
+    int next_aux = 0;
+    for (size_t gi = 0; gi < groups_.size(); ++gi) {
+        const LaunchGroup& g = groups_[gi];
+        if (g.n == 0) continue;
+        cudaStream_t st = stream_;
+        if (g.kind == 0) {
+            st = aux_[next_aux];
+            next_aux = (next_aux + 1) % (int)aux_.size();
+        }
+        cudaError_t e;
+        if (g.kind == 0) {
+            if (g.fp32) {
+                SmallArgs<float> a{d_pairs_.p, d_rec32_.p, d_jk_tasks_.p + g.off, (int)g.n, d_boys32_.p,
+                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2};
+                e = launch_small_f32(g.pcb, g.pck, &a, nk, st);
+            } else {
+                SmallArgs<double> a{d_pairs_.p, d_rec64_.p, d_jk_tasks_.p + g.off, (int)g.n, d_boys_.p,
+                                    opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2};
+                e = launch_small_f64(g.pcb, g.pck, &a, nk, st);
+            }
+        } else {
+            if (g.fp32) {
+                WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
+                                  d_jk_tasks_.p + g.off, (int)g.n, d_counters_.p + gi, d_boys32_.p,
+                                  opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
+                e = launch_warp(true, &a, nk, g.grid, g.warps_per_cta, st);
+            } else {
+                WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
+                                   d_jk_tasks_.p + g.off, (int)g.n, d_counters_.p + gi, d_boys_.p,
+                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
+                e = launch_warp(false, &a, nk, g.grid, g.warps_per_cta, st);
+            }
+        }
+        cuda_check(e, "class kernel launch");
+    }
+    for (size_t s2 = 0; s2 < aux_.size(); ++s2) {
+        cuda_check(cudaEventRecord(aux_ev_[s2], aux_[s2]), "join");
+        cuda_check(cudaStreamWaitEvent(stream_, aux_ev_[s2], 0), "join wait");
+    }
+}
+
 void Job::record_stats(int launches)
 {
     float ms = 0.f, kms = 0.f;
@@ -282,10 +524,10 @@ void Job::record_stats(int launches)
     stats.ms = ms;
     stats.kernel_ms = kms;
     stats.quartets = ntasks_;
-    stats.quartets_fp32 = 0;
+    stats.quartets_fp32 = quartets32_;
     stats.prim_quartets = prim_quartets_;
     stats.flops_fp64 = flops_;
-    stats.flops_fp32 = 0;
+    stats.flops_fp32 = flops32_;
     stats.launches = launches;
 }
 
@@ -296,21 +538,16 @@ void Job::fock_rhf_device(const double* dP, double* dG)
     size_t n = (size_t)K * K;
     d_J_.alloc(n);
     d_K_.alloc(n);
+    cuda_check(cudaEventRecord(ev0_, stream_), "event");
     cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
-    LaunchArgs a = base_args();
-    a.Dj = dP;
-    a.Dk = dP;
-    a.Jacc = d_J_.p;
-    a.Kacc = d_K_.p;
-    cuda_check(cudaEventRecord(ev0_, stream_), "event");
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    run_tasks(MODE_JK, 1, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    launch_jk(1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    record_stats(2);
+    record_stats((int)groups_.size() + 1);
 }
 
 void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb)
@@ -322,25 +559,18 @@ void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, doub
     d_K_.alloc(n);
     d_K2_.alloc(n);
     d_Dj_.alloc(n);
+    cuda_check(cudaEventRecord(ev0_, stream_), "event");
     cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(d_K2_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaEventRecord(ev0_, stream_), "event");
     cuda_check(launch_add(dPa, dPb, d_Dj_.p, (int)n, stream_), "add");
-    LaunchArgs a = base_args();
-    a.Dj = d_Dj_.p;
-    a.Dk = dPa;
-    a.Dk2 = dPb;
-    a.Jacc = d_J_.p;
-    a.Kacc = d_K_.p;
-    a.Kacc2 = d_K2_.p;
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    run_tasks(MODE_JK, 2, nullptr, d_tasks_, ntasks_, maxacc_, maxw_, maxr_, a);
+    launch_jk(2, d_Dj_.p, dPa, dPb, d_J_.p, d_K_.p, d_K2_.p);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_uhf(d_J_.p, d_K_.p, d_K2_.p, dJ, dKa, dKb, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    record_stats(3);
+    record_stats((int)groups_.size() + 2);
 }
 
 void Job::fock_rhf(const double* P, double* G)

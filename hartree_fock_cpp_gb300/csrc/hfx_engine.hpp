@@ -19,6 +19,11 @@ cudaError_t launch_finish_rhf(const double* Jacc, const double* Kacc, double* G,
 cudaError_t launch_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
                               double* Kbo, int K, cudaStream_t st);
 cudaError_t launch_add(const double* A, const double* B, double* C, int n, cudaStream_t st);
+cudaError_t launch_small_f64(int pcb, int pck, const void* args, int nk, cudaStream_t st);
+cudaError_t launch_small_f32(int pcb, int pck, const void* args, int nk, cudaStream_t st);
+cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
+int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
+bool is_small_class(int pcb, int pck);
 
 void cuda_check(cudaError_t e, const char* what);
 
@@ -72,6 +77,27 @@ struct PairData {
     std::vector<DPair> dpairs;
     std::vector<PairGeo> geo;
     std::vector<double> epool;
+    std::vector<double> rec;   // class-kernel primitive-pair records
+};
+
+// Per pair class: component-pair / coefficient layout of the records.
+struct ClassTables {
+    std::vector<PairClassTab> tab;
+    std::vector<int> ab_start;
+    std::vector<short> k_herm, k_lin;
+};
+const ClassTables& class_tables();
+
+// One kernel launch of a Fock build.
+struct LaunchGroup {
+    int kind;            // 0: small-class kernel, 1: warp kernel
+    int pcb, pck;        // small-class kernel class
+    bool fp32;
+    int slice;           // warp kernel: per-warp slice (elements)
+    int warps_per_cta;
+    int grid;
+    size_t off, n;       // task range in the concatenated list
+    double flops, prims;
 };
 PairData build_pair_data(const Basis& b);
 
@@ -111,7 +137,24 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evk0_ = nullptr, evk1_ = nullptr;
 
+    void build_jk_groups();
+    void launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
+                   double* Kx2);
+
     std::vector<HostPair> hpairs_;
+    std::vector<LaunchGroup> groups_;
+    DevBuf<Task> d_jk_tasks_;
+    DevBuf<int> d_counters_;
+    DevBuf<double> d_rec64_;
+    DevBuf<float> d_rec32_;
+    DevBuf<float> d_boys32_;
+    DevBuf<PairClassTab> d_pct_;
+    DevBuf<int> d_abs_;
+    DevBuf<short> d_kh_, d_kl_;
+    std::vector<cudaStream_t> aux_;
+    std::vector<cudaEvent_t> aux_ev_;
+    cudaEvent_t fork_ev_ = nullptr;
+    double flops32_ = 0.0, quartets32_ = 0.0;
     std::vector<double> qsh_;     // per pair
     std::vector<double> qbf_;     // per BF pair
     DevBuf<DPair> d_pairs_;

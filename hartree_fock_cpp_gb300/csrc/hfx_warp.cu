@@ -1,0 +1,387 @@
+// hfx_warp.cu -- warp-per-shell-quartet McMurchie-Davidson kernel with direct
+// J/K digestion, for any angular-momentum class (runtime L), FP64 or FP32.
+//
+// Each warp takes shell quartets from a global work queue and works on its own
+// slice of shared memory; there are no CTA-wide barriers.  Per bra primitive
+// pair ij the warp accumulates the ket-transformed Hermite integrals
+//   W[tuv][cd] = sum_kl sum_{tnp in nz(cd)} (-1)^{|tnp|} c^{kl}_{cd,tnp} R^{ij,kl}[tuv+tnp]
+// over all ket primitive pairs, then applies the bra transform once:
+//   acc[ab][cd] += sum_{tuv in nz(ab)} c^{ij}_{ab,tuv} W[tuv][cd]
+// so the bra work is amortised over the ket contraction (the reference
+// re-does the full Hermite sum per primitive quartet and per basis-function
+// quartet, integrals.hpp:675-698).  Only structurally non-zero
+// Hermite->Cartesian coefficients are stored and used.
+//
+// R_{tuv} (stage 1) is computed either one primitive quartet per lane
+// (lane-parallel, for batches of ket primitives) or level-parallel across the
+// warp for single primitive quartets; both use the in-place downward
+// recursion over m of integrals.hpp:541-618, driven by a neighbour table.
+#include <cuda_runtime.h>
+
+#include "hfx_device.cuh"
+
+namespace hfx {
+
+
+__host__ __device__ constexpr int w_nh(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }
+__host__ __device__ constexpr int w_nc(int l) { return (l + 1) * (l + 2) / 2; }
+
+template <typename T>
+__device__ __forceinline__ T w_fma(T a, T b, T c)
+{
+    return fma(a, b, c);
+}
+
+// F_L(T) by Taylor from the table, e^{-T}; or asymptotic values beyond it.
+template <typename T>
+__device__ __forceinline__ void boys_top(T Tv, int L, const T* __restrict__ tab, T& FL, T& e, bool& table)
+{
+    if (Tv < (T)kBoysTMax) {
+        table = true;
+        int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
+        T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+        const T* f = tab + k * kBoysM + L;
+        T r;
+        if (sizeof(T) == 8) {
+            r = __ldg(f + 6) * (T)(1.0 / 720.0);
+            r = w_fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
+            r = w_fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
+        } else {
+            r = __ldg(f + 4) * (T)(1.0 / 24.0);
+        }
+        r = w_fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
+        r = w_fma(r, nd, __ldg(f + 2) * (T)0.5);
+        r = w_fma(r, nd, __ldg(f + 1));
+        FL = w_fma(r, nd, __ldg(f));
+        // exp(-T) = exp(-T_k) exp(nd), |nd| <= 1/32
+        T x;
+        if (sizeof(T) == 8) {
+            x = (T)(1.0 / 5040.0);
+            x = w_fma(x, nd, (T)(1.0 / 720.0));
+            x = w_fma(x, nd, (T)(1.0 / 120.0));
+            x = w_fma(x, nd, (T)(1.0 / 24.0));
+        } else {
+            x = (T)(1.0 / 24.0);
+        }
+        x = w_fma(x, nd, (T)(1.0 / 6.0));
+        x = w_fma(x, nd, (T)0.5);
+        x = w_fma(x, nd, (T)1);
+        x = w_fma(x, nd, (T)1);
+        e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+    } else {
+        table = false;
+        FL = (T)0;
+        e = (sizeof(T) == 8 && L >= 5) ? (T)exp(-(double)Tv) : (T)0;
+    }
+}
+
+// Seeds s_m = pref (-2 rho)^m F_m(T), m = 0..L, written to S[m * sstride].
+template <typename T>
+__device__ __forceinline__ void boys_seeds(T Tv, T rho, T pref, int L, const T* __restrict__ tab, T* S, int sstride)
+{
+    T FL, e;
+    bool table;
+    boys_top<T>(Tv, L, tab, FL, e, table);
+    T m2r = (T)-2 * rho;
+    if (table) {
+        // downward F_m = (2T F_{m+1} + e) / (2m+1); the power of (-2 rho) built upward
+        T F = FL;
+        T pw = pref;
+        for (int m = 0; m < L; ++m) pw *= m2r;
+        S[L * sstride] = pw * F;
+        T t2 = Tv + Tv;
+        T rm2r = (T)1 / m2r;
+        for (int m = L - 1; m >= 0; --m) {
+            F = w_fma(t2, F, e) * ((T)1 / (T)(2 * m + 1));
+            pw *= rm2r;
+            S[m * sstride] = pw * F;
+        }
+    } else {
+        T rs = rsqrt(Tv);
+        T F = (T)0.88622692545275801365 * rs;
+        T inv2T = (T)0.5 * rs * rs;
+        T pw = pref;
+        S[0] = pw * F;
+        for (int m = 0; m < L; ++m) {
+            F = ((T)(2 * m + 1) * F - e) * inv2T;
+            pw *= m2r;
+            S[(m + 1) * sstride] = pw * F;
+        }
+    }
+}
+
+// In-place recursion for the table R[e * rs] (e in packed Hermite order).
+// nb[e] = dir | i1 << 2 | i2 << 11 | c2 << 20  (dir 0/1/2 = x/y/z).
+template <typename T>
+__device__ __forceinline__ void recur_lane(T X, T Y, T Z, int L, const T* S, int sstride, T* R, int rs,
+                                           const int* nb)
+{
+    R[0] = S[L * sstride];
+    for (int n = L - 1; n >= 0; --n) {
+        int top = w_nh(L - n);
+        for (int e = top - 1; e >= 1; --e) {
+            int w = nb[e];
+            int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511, c2 = (w >> 20) & 15;
+            T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
+            T val = xd * R[i1 * rs];
+            if (c2) val = w_fma((T)c2, R[i2 * rs], val);
+            R[e * rs] = val;
+        }
+        R[0] = S[n * sstride];
+    }
+}
+
+__device__ __forceinline__ long long wpidx(int a, int b)
+{
+    int hi = a > b ? a : b, lo = a > b ? b : a;
+    return (long long)hi * (hi + 1) / 2 + lo;
+}
+
+template <typename T, int NK>
+__global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    short* idx3 = reinterpret_cast<short*>(smem);                 // 2197 shorts (4394 B)
+    int* nbt = reinterpret_cast<int*>(smem + 4400);               // 455 ints (1820 B) -> 6220
+    int* clin = reinterpret_cast<int*>(smem + 6240);              // 455 ints -> 8060
+    T* wbase = reinterpret_cast<T*>(smem + 8064);
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    T* sl = wbase + (size_t)warp * a.slice;
+
+    for (int e = threadIdx.x; e < 2197; e += blockDim.x) {
+        int t = e / 169, u = (e / 13) % 13, v = e % 13;
+        int s = t + u + v;
+        idx3[e] = (short)(s <= 12 ? s * (s + 1) * (s + 2) / 6 + t * (s + 1) - t * (t - 1) / 2 + u : -1);
+    }
+    for (int e = threadIdx.x; e < 455; e += blockDim.x) {
+        int s = 0;
+        while (w_nh(s) <= e) ++s;
+        int o = e - (s == 0 ? 0 : w_nh(s - 1));
+        int t = 0;
+        while (o >= s - t + 1) {
+            o -= s - t + 1;
+            ++t;
+        }
+        int u = o, v = s - t - u;
+        clin[e] = t * 169 + u * 13 + v;
+        int w = 0;
+        if (s > 0) {
+            auto h = [](int tt, int uu, int vv) {
+                int ss = tt + uu + vv;
+                return ss * (ss + 1) * (ss + 2) / 6 + tt * (ss + 1) - tt * (tt - 1) / 2 + uu;
+            };
+            int dir, i1, i2 = 0, c2 = 0;
+            if (t > 0) {
+                dir = 0;
+                i1 = h(t - 1, u, v);
+                if (t > 1) { i2 = h(t - 2, u, v); c2 = t - 1; }
+            } else if (u > 0) {
+                dir = 1;
+                i1 = h(t, u - 1, v);
+                if (u > 1) { i2 = h(t, u - 2, v); c2 = u - 1; }
+            } else {
+                dir = 2;
+                i1 = h(t, u, v - 1);
+                if (v > 1) { i2 = h(t, u, v - 2); c2 = v - 1; }
+            }
+            w = dir | (i1 << 2) | (i2 << 11) | (c2 << 20);
+        }
+        nbt[e] = w;
+    }
+    __syncthreads();
+
+    const T* __restrict__ rec = a.rec;
+    while (true) {
+        int tk = 0;
+        if (lane == 0) tk = atomicAdd(a.counter, 1);
+        tk = __shfl_sync(0xffffffffu, tk, 0);
+        if (tk >= a.ntasks) break;
+        const Task task = a.tasks[tk];
+        const DPair bra = a.pairs[task.bra];
+        const DPair ket = a.pairs[task.ket];
+        const PairClassTab cb = a.pct[bra.pc];
+        const PairClassTab ck = a.pct[ket.pc];
+        const int L1 = bra.l0 + bra.l1, L2 = ket.l0 + ket.l1, L = L1 + L2;
+        const int n1 = w_nc(bra.l1), n3 = w_nc(ket.l1);
+        const int nab = cb.nab, ncd = ck.nab;
+        const int H1 = w_nh(L1), HL = w_nh(L);
+        const int nout = nab * ncd, nw = H1 * ncd;
+        const int* abs_b = a.ab_start + cb.ab_off;
+        const int* abs_k = a.ab_start + ck.ab_off;
+        const short* kh_b = a.k_herm + cb.k_off;
+        const short* kl_k = a.k_lin + ck.k_off;
+        // slice layout: acc[nout] W[nw] then the R area
+        T* acc = sl;
+        T* W = acc + nout;
+        T* Ra = W + nw;
+        const bool lane_mode = a.lane_r && L <= 6 && ket.npp >= 6;
+        T* Sd = Ra + (lane_mode ? HL * 32 : 2 * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
+        for (int e = lane; e < nout; e += 32) acc[e] = (T)0;
+
+        for (int ij = 0; ij < bra.npp; ++ij) {
+            const T* rb = rec + bra.rec_off + (long long)ij * cb.stride;
+            const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
+            for (int e = lane; e < nw; e += 32) W[e] = (T)0;
+            __syncwarp();
+            if (lane_mode) {
+                for (int kl0 = 0; kl0 < ket.npp; kl0 += 32) {
+                    const int nb = min(32, ket.npp - kl0);
+                    if (lane < nb) {
+                        const T* rk = rec + ket.rec_off + (long long)(kl0 + lane) * ck.stride;
+                        const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
+                        const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+                        const T pq = p + q;
+                        const T rho = p * q / pq;
+                        const T Tv = rho * (X * X + Y * Y + Z * Z);
+                        const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
+                        boys_seeds<T>(Tv, rho, pref, L, a.boys, Sd + lane, 32);
+                        recur_lane<T>(X, Y, Z, L, Sd + lane, 32, Ra + lane, 32, nbt);
+                    }
+                    __syncwarp();
+                    // stage 2: W[tuv][cd] += sum_b sum_k (+-) c_k R_b[tuv + tnp_k]
+                    for (int e = lane; e < nw; e += 32) {
+                        const int tuv = e / ncd, cd = e - tuv * ncd;
+                        const int lt = clin[tuv];
+                        const int k0 = __ldg(abs_k + cd), k1 = __ldg(abs_k + cd + 1);
+                        T s = (T)0;
+                        for (int b = 0; b < nb; ++b) {
+                            const T* ck_ = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride + 4;
+                            for (int k = k0; k < k1; ++k) {
+                                const int w = __ldg(kl_k + k);
+                                const T r = Ra[idx3[lt + (w & 16383)] * 32 + b];
+                                const T c = __ldg(ck_ + k);
+                                s = (w & 16384) ? w_fma(-c, r, s) : w_fma(c, r, s);
+                            }
+                        }
+                        W[e] += s;
+                    }
+                    __syncwarp();
+                }
+            } else {
+                for (int kl = 0; kl < ket.npp; ++kl) {
+                    const T* rk = rec + ket.rec_off + (long long)kl * ck.stride;
+                    const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
+                    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+                    const T pq = p + q;
+                    const T rho = p * q / pq;
+                    const T Tv = rho * (X * X + Y * Y + Z * Z);
+                    const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
+                    // seeds: lane 0 (downward recursion is sequential in m)
+                    if (lane == 0) boys_seeds<T>(Tv, rho, pref, L, a.boys, Sd, 1);
+                    __syncwarp();
+                    // level-parallel recursion, ping-pong between Ra and Rb
+                    T* prev = Ra;
+                    T* cur = Ra + HL;
+                    if (lane == 0) prev[0] = Sd[L];
+                    __syncwarp();
+                    for (int n = L - 1; n >= 0; --n) {
+                        const int cnt = w_nh(L - n);
+                        for (int e = lane; e < cnt; e += 32) {
+                            T val;
+                            if (e == 0) {
+                                val = Sd[n];
+                            } else {
+                                const int w = nbt[e];
+                                const int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511, c2 = (w >> 20) & 15;
+                                const T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
+                                val = xd * prev[i1];
+                                if (c2) val = w_fma((T)c2, prev[i2], val);
+                            }
+                            cur[e] = val;
+                        }
+                        __syncwarp();
+                        T* tmp = prev;
+                        prev = cur;
+                        cur = tmp;
+                    }
+                    const T* ck_ = rk + 4;
+                    for (int e = lane; e < nw; e += 32) {
+                        const int tuv = e / ncd, cd = e - tuv * ncd;
+                        const int lt = clin[tuv];
+                        const int k0 = __ldg(abs_k + cd), k1 = __ldg(abs_k + cd + 1);
+                        T s = (T)0;
+                        for (int k = k0; k < k1; ++k) {
+                            const int w = __ldg(kl_k + k);
+                            const T r = prev[idx3[lt + (w & 16383)]];
+                            const T c = __ldg(ck_ + k);
+                            s = (w & 16384) ? w_fma(-c, r, s) : w_fma(c, r, s);
+                        }
+                        W[e] += s;
+                    }
+                    __syncwarp();
+                }
+            }
+            // stage 3: bra transform, once per bra primitive pair
+            const T* cbp = rb + 4;
+            for (int e = lane; e < nout; e += 32) {
+                const int ab = e / ncd, cd = e - ab * ncd;
+                const int k0 = __ldg(abs_b + ab), k1 = __ldg(abs_b + ab + 1);
+                T s = (T)0;
+                for (int k = k0; k < k1; ++k) s = w_fma(__ldg(cbp + k), W[__ldg(kh_b + k) * ncd + cd], s);
+                acc[e] += s;
+            }
+            __syncwarp();
+        }
+
+        // digestion (FP64)
+        const int K = a.K;
+        for (int e = lane; e < nout; e += 32) {
+            const int ab = e / ncd, cd = e - ab * ncd;
+            const int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
+            const int i = bra.bf0 + ia, j = bra.bf1 + ib, k = ket.bf0 + ic, l = ket.bf1 + id;
+            if (bra.same && ia < ib) continue;
+            if (ket.same && ic < id) continue;
+            const long long pij = wpidx(i, j), pkl = wpidx(k, l);
+            if (task.bra == task.ket && pij < pkl) continue;
+            if (a.thr >= 0.0 && __ldg(a.Qbf + pij) * __ldg(a.Qbf + pkl) < a.thr) continue;
+            double v = (double)acc[e] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
+            atomicAdd(a.J + (long long)i * K + j, __ldg(a.Dj + (long long)k * K + l) * v);
+            atomicAdd(a.J + (long long)k * K + l, __ldg(a.Dj + (long long)i * K + j) * v);
+            atomicAdd(a.Kx + (long long)i * K + k, __ldg(a.Dk + (long long)j * K + l) * v);
+            atomicAdd(a.Kx + (long long)j * K + l, __ldg(a.Dk + (long long)i * K + k) * v);
+            atomicAdd(a.Kx + (long long)i * K + l, __ldg(a.Dk + (long long)j * K + k) * v);
+            atomicAdd(a.Kx + (long long)j * K + k, __ldg(a.Dk + (long long)i * K + l) * v);
+            if (NK == 2) {
+                atomicAdd(a.Kx2 + (long long)i * K + k, __ldg(a.Dk2 + (long long)j * K + l) * v);
+                atomicAdd(a.Kx2 + (long long)j * K + l, __ldg(a.Dk2 + (long long)i * K + k) * v);
+                atomicAdd(a.Kx2 + (long long)i * K + l, __ldg(a.Dk2 + (long long)j * K + k) * v);
+                atomicAdd(a.Kx2 + (long long)j * K + k, __ldg(a.Dk2 + (long long)i * K + l) * v);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// slice size (T elements) a task needs
+int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r)
+{
+    int L1 = l0b + l1b, L2 = l0k + l1k, L = L1 + L2;
+    int nab = w_nc(l0b) * w_nc(l1b), ncd = w_nc(l0k) * w_nc(l1k);
+    int HL = w_nh(L);
+    bool lane_mode = lane_r && L <= 6 && npp_ket >= 6;
+    int r = lane_mode ? HL * 32 + (L + 1) * 32 : 2 * HL + (L + 1);
+    return nab * ncd + w_nh(L1) * ncd + r;
+}
+
+template <typename T>
+cudaError_t launch_warp_t(const WarpArgs<T>& a, int nk, int grid, int warps_per_cta, cudaStream_t st)
+{
+    size_t sm = 8064 + sizeof(T) * (size_t)a.slice * warps_per_cta;
+    auto go = [&](auto kern) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, 32 * warps_per_cta, sm, st>>>(a);
+        return cudaGetLastError();
+    };
+    if (nk == 2) return go(k_warp_quartet<T, 2>);
+    return go(k_warp_quartet<T, 1>);
+}
+
+cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st)
+{
+    if (fp32) return launch_warp_t<float>(*(const WarpArgs<float>*)args, nk, grid, warps_per_cta, st);
+    return launch_warp_t<double>(*(const WarpArgs<double>*)args, nk, grid, warps_per_cta, st);
+}
+
+}  // namespace hfx
