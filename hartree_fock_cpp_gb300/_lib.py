@@ -86,6 +86,7 @@ SIGNATURES = {
     "hfx_fock_uhf": (I, [V, V, V, V, V, V]),
     "hfx_fock_rhf_device": (I, [V, V, V]),
     "hfx_fock_uhf_device": (I, [V, V, V, V, V, V]),
+    "hfx_fock_rhf_device_noalloc": (I, [V, V, V]),
     "hfx_eri_unique": (I, [V, D, V]),
     "hfx_eri_gpu": (I, [V, D, V]),
     "hfx_job_rhf": (I, [V, V, V, V, V, V, V]),

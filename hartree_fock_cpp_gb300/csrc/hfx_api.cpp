@@ -15,6 +15,7 @@ struct hfx_job {
 };
 
 namespace hfx {
+void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG);   // hfx_noalloc.cu
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace hfx
@@ -213,6 +214,14 @@ hfx_status hfx_fock_uhf_device(hfx_job* job, const double* dPa, const double* dP
     return guarded([&] {
         if (!job || !dPa || !dPb || !dJ || !dKa || !dKb) throw Error(HFX_ERR_INVALID, "null argument");
         job->job->fock_uhf_device(dPa, dPb, dJ, dKa, dKb);
+    });
+}
+
+hfx_status hfx_fock_rhf_device_noalloc(hfx_job* job, const double* dP, double* dG)
+{
+    return guarded([&] {
+        if (!job || !dP || !dG) throw Error(HFX_ERR_INVALID, "null argument");
+        fock_rhf_noalloc(*job->job, job->job->device(), dP, dG);
     });
 }
 

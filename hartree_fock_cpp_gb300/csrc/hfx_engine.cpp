@@ -469,9 +469,10 @@ void Job::build_jk_groups()
 }
 
 void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
-                    double* Kx2)
+                    double* Kx2, int* counters)
 {
-    cuda_check(cudaMemsetAsync(d_counters_.p, 0, sizeof(int) * d_counters_.n, stream_), "memset counters");
+    int* ctr = counters ? counters : d_counters_.p;
+    cuda_check(cudaMemsetAsync(ctr, 0, sizeof(int) * d_counters_.n, stream_), "memset counters");
     cuda_check(cudaEventRecord(fork_ev_, stream_), "fork");
     for (auto st : aux_) cuda_check(cudaStreamWaitEvent(st, fork_ev_, 0), "fork wait");
     // warp groups (the long ones) on the main stream, small classes spread over the others
@@ -498,12 +499,12 @@ void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk
         } else {
             if (g.fp32) {
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
-                                  d_jk_tasks_.p + g.off, (int)g.n, d_counters_.p + gi, d_boys32_.p,
+                                  d_jk_tasks_.p + g.off, (int)g.n, ctr + gi, d_boys32_.p,
                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
                 e = launch_warp(true, &a, nk, g.grid, g.warps_per_cta, st);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
-                                   d_jk_tasks_.p + g.off, (int)g.n, d_counters_.p + gi, d_boys_.p,
+                                   d_jk_tasks_.p + g.off, (int)g.n, ctr + gi, d_boys_.p,
                                    opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
                 e = launch_warp(false, &a, nk, g.grid, g.warps_per_cta, st);
             }
@@ -545,6 +546,23 @@ void Job::fock_rhf_device(const double* dP, double* dG)
     launch_jk(1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
+    cuda_check(cudaEventRecord(ev1_, stream_), "event");
+    cuda_check(cudaStreamSynchronize(stream_), "fock build");
+    record_stats((int)groups_.size() + 1);
+}
+
+void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, double* Kacc, int* counters)
+{
+    cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    int K = basis_.K;
+    size_t n = (size_t)K * K;
+    cuda_check(cudaEventRecord(ev0_, stream_), "event");
+    cuda_check(cudaMemsetAsync(Jacc, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaMemsetAsync(Kacc, 0, n * sizeof(double), stream_), "memset");
+    cuda_check(cudaEventRecord(evk0_, stream_), "event");
+    launch_jk(1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters);
+    cuda_check(cudaEventRecord(evk1_, stream_), "event");
+    cuda_check(launch_finish_rhf(Jacc, Kacc, dG, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats((int)groups_.size() + 1);

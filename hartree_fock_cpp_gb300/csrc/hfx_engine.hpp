@@ -107,11 +107,17 @@ public:
     ~Job();
 
     int K() const { return basis_.K; }
+    int device() const { return device_; }
     const Basis& basis() const { return basis_; }
 
     void schwarz_host(std::vector<double>& Qbf) const;
     // device-pointer Fock builds (synchronous)
     void fock_rhf_device(const double* dP, double* dG);
+    // RHF build whose scratch (J/K accumulators, work-queue counters) is
+    // supplied by the caller; allocates nothing.  Jacc/Kacc hold K*K doubles,
+    // counters num_launch_groups() ints.
+    void fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, double* Kacc, int* counters);
+    int num_launch_groups() const { return (int)groups_.size(); }
     void fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb);
     void fock_rhf(const double* P, double* G);
     void fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb);
@@ -139,7 +145,7 @@ private:
 
     void build_jk_groups();
     void launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
-                   double* Kx2);
+                   double* Kx2, int* counters = nullptr);
 
     std::vector<HostPair> hpairs_;
     std::vector<LaunchGroup> groups_;

@@ -128,6 +128,18 @@ hfx_status hfx_fock_rhf_device(hfx_job *job, const double *dP, double *dG);
 hfx_status hfx_fock_uhf_device(hfx_job *job, const double *dPa, const double *dPb, double *dJ,
                                double *dKa, double *dKb);
 
+/* RHF two-electron matrix like hfx_fock_rhf_device, for callers that cannot
+ * allocate device memory at call time (an application whose own allocator
+ * owns the GPU memory, or a loop that must not let cudaMalloc synchronise
+ * the device).  No counterpart in the reference.  It allocates nothing: its
+ * scratch (J/K accumulators, work-queue counters) lives in one static device
+ * array of about 4 MB, reserved on every device that loads the library.
+ * Limits: K <= 512, else HFX_ERR_UNSUPPORTED.  The first call on a device
+ * resolves that array's address; make it before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race; serialise
+ * them.  The job itself must already exist (hfx_create allocates). */
+hfx_status hfx_fock_rhf_device_noalloc(hfx_job *job, const double *dP, double *dG);
+
 /* All unique ERIs in the reference's packed layout: out[eri_index(i,j,k,l)],
  * P(P+1)/2 doubles with P = K(K+1)/2, zero where Q_ij*Q_kl < threshold
  * (integrals.hpp:754-787 / cuda/src/eri.cu:20-89). */
