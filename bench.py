@@ -258,6 +258,43 @@ def run_engine(args):
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     peak = fp64_peak / 1e3
 
+    # ---- mixed vs FP64 Fock builds on n-decane/6-31G* ------------------------
+    mixed = None
+    if not args.no_mixed:
+        cfg_d = W.n_decane()
+        r64 = H.rhf_diis(cfg_d, "6-31G*", **scf_kw)
+        Pd = r64["density"]
+        Kd = Pd.shape[0]
+        fbm = H.FockBuilder(config=cfg_d, basis_set="6-31G*", device=local)
+        tau, dE_proxy, _, _ = fbm.autotune_fp32_threshold(Pd, 2.5e-7)
+        fb64 = H.FockBuilder(config=cfg_d, basis_set="6-31G*", device=local)
+        dPd = torch.tensor(Pd, device="cuda", dtype=torch.float64)
+        dG64 = torch.zeros_like(dPd)
+        dGmx = torch.zeros_like(dPd)
+        tms = {}
+        for name, f, out in (("fp64", fb64, dG64), ("mixed", fbm, dGmx)):
+            f.repulsion_matrix_device(dPd.data_ptr(), out.data_ptr())
+            ts = []
+            for _ in range(max(3, args.steps)):
+                flush_l2(torch, flush)
+                torch.cuda.synchronize()
+                f.repulsion_matrix_device(dPd.data_ptr(), out.data_ptr())
+                ts.append(f.stats()["ms"])
+            tms[name] = float(np.mean(ts))
+        smx = fbm.stats()
+        max_dF = float((dGmx - dG64).abs().max().item())
+        rmx = H.rhf_diis(cfg_d, "6-31G*", precision=H.HFX_PREC_MIXED, fp32_threshold=tau, **scf_kw)
+        mixed = {"workload": "n-decane C10H22 RHF/6-31G* (K=%d), seed 20261203 noise 0.05 bohr" % Kd,
+                 "fp32_threshold": tau, "autotune_target_dE": 2.5e-7, "autotune_dE": dE_proxy,
+                 "fock_builds_per_s_fp64": 1e3 / tms["fp64"], "fock_builds_per_s_mixed": 1e3 / tms["mixed"],
+                 "speedup": tms["fp64"] / tms["mixed"], "fp32_quartet_fraction": smx["quartets_fp32"] / smx["quartets"],
+                 "max_dF_vs_fp64": max_dF, "scf_dE_vs_fp64": rmx["E_tot"] - r64["E_tot"],
+                 "scf_iterations_fp64": r64["iterations"], "scf_iterations_mixed": rmx["iterations"],
+                 "scf_fock_ms_fp64": r64["fock_ms"], "scf_fock_ms_mixed": rmx["fock_ms"],
+                 "scf_builds_mixed_fp64_delta": [rmx["mixed_builds"], rmx["fp64_builds"], rmx["delta_builds"]]}
+        fbm.close()
+        fb64.close()
+
     # ---- e2e: through hfx_rhf_diis with host buffers -------------------------
     e2e_lat = []
     r = None
@@ -299,7 +336,8 @@ def run_engine(args):
                    "K": K, "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between steps (512 MB)"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
-        "fock_builds_per_s": {"fp64": 1e3 / build_ms, "mixed": None},
+        "fock_builds_per_s": {"fp64": 1e3 / build_ms},
+        "mixed_precision": mixed,
         "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP64 FMA-loop peak of this GPU (hfx_measure_peaks, same run)",
@@ -343,6 +381,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision section")
     ap.add_argument("--fock-only", action="store_true",
                     help="profiling case: job setup + --builds device Fock builds of --molecule/--basis")
     ap.add_argument("--molecule", default="benzene", choices=["water", "benzene", "n_decane"])

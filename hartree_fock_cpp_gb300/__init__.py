@@ -158,6 +158,16 @@ class FockBuilder:
         check(lib.hfx_eri_unique(self._job, threshold, ptr(out)))
         return out
 
+    def autotune_fp32_threshold(self, P, target_dE=2.5e-7):
+        """Largest FP32 Schwarz cut keeping |dE| at density P within target_dE;
+        switches this job to mixed precision at it.  Returns (tau, dE,
+        ms_fp64, ms_mixed)."""
+        P = self._mat(P)
+        t, d, a, b = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib.hfx_autotune_fp32_threshold(self._job, ptr(P), target_dE, ctypes.byref(t), ctypes.byref(d),
+                                              ctypes.byref(a), ctypes.byref(b)))
+        return t.value, d.value, a.value, b.value
+
     def stats(self):
         s = _lib.BuildStats()
         check(lib.hfx_last_build_stats(self._job, ctypes.byref(s)))
@@ -224,8 +234,8 @@ def rhf_diis(config, basis_set, param_path=None, charge=0, eri_device="GPU", set
         check(st)
     return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
                 K=r.K, Ne=r.n_electrons, density=dens, coefficient=coef, mo_energy=mo, duration=r.seconds,
-                fock_ms=r.fock_ms, fock_builds=r.fock_builds, hardware=eri_device, BasisSet=basis_set,
-                charge=charge)
+                fock_ms=r.fock_ms, fock_builds=r.fock_builds, mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds,
+                delta_builds=r.delta_builds, hardware=eri_device, BasisSet=basis_set, charge=charge)
 
 
 def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_device="GPU",
@@ -254,7 +264,8 @@ def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_
         check(st)
     return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
                 K=r.K, Pa=Pa, Pb=Pb, Ea=ea, Eb=eb, duration=r.seconds, fock_ms=r.fock_ms,
-                fock_builds=r.fock_builds, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
+                fock_builds=r.fock_builds, mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds,
+                delta_builds=r.delta_builds, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
                 BasisSet=basis_set, charge=charge)
 
 

@@ -60,7 +60,8 @@ class ScfResult(ctypes.Structure):
     _fields_ = [("E_tot", ctypes.c_double), ("E_ele", ctypes.c_double), ("E_nuc", ctypes.c_double),
                 ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("K", ctypes.c_int),
                 ("n_electrons", ctypes.c_int), ("seconds", ctypes.c_double), ("fock_ms", ctypes.c_double),
-                ("fock_builds", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("fock_builds", ctypes.c_int), ("mixed_builds", ctypes.c_int), ("fp64_builds", ctypes.c_int),
+                ("delta_builds", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 G_BUILDER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
@@ -92,6 +93,7 @@ SIGNATURES = {
     "hfx_job_rhf": (I, [V, V, V, V, V, V, V]),
     "hfx_job_uhf": (I, [V, V, I, I, V, V, V, V, V]),
     "hfx_last_build_stats": (I, [V, V]),
+    "hfx_autotune_fp32_threshold": (I, [V, V, D, P(D), P(D), P(D), P(D)]),
     "hfx_rhf_diis": (I, [V, V, V, V, V, V, V]),
     "hfx_uhf_diis": (I, [V, V, I, I, V, V, V, V, V, V, V]),
     "hfx_rhf_diis_with_builder": (I, [V, V, V, G_BUILDER, V, V, V, V]),

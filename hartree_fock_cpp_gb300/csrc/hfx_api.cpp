@@ -15,6 +15,9 @@ struct hfx_job {
 };
 
 namespace hfx {
+// density-weighted screening threshold of the FP64 builds of density changes
+// in the mixed-precision SCF (Q_AB Q_CD max|dD| below this: quartet skipped)
+constexpr double kDeltaThr = 1e-10;
 void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG);   // hfx_noalloc.cu
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -244,6 +247,17 @@ hfx_status hfx_eri_gpu(const hfx_functions* basis, double threshold, double* out
     });
 }
 
+hfx_status hfx_autotune_fp32_threshold(hfx_job* job, const double* P, double target_dE, double* tau,
+                                       double* dE, double* ms_fp64, double* ms_mixed)
+{
+    return guarded([&] {
+        if (!job || !P) throw Error(HFX_ERR_INVALID, "null argument");
+        if (!(target_dE > 0.0)) throw Error(HFX_ERR_INVALID, "target_dE must be positive");
+        double t = job->job->autotune_fp32_threshold(P, target_dE, dE, ms_fp64, ms_mixed);
+        if (tau) *tau = t;
+    });
+}
+
 hfx_status hfx_last_build_stats(const hfx_job* job, hfx_build_stats* stats)
 {
     return guarded([&] {
@@ -266,6 +280,9 @@ static void fill_result(const ScfOutput& o, hfx_scf_result* r, double fock_ms)
     r->seconds = o.seconds;
     r->fock_ms = fock_ms;
     r->fock_builds = o.fock_builds;
+    r->mixed_builds = o.mixed_builds;
+    r->fp64_builds = o.fp64_builds;
+    r->delta_builds = o.delta_builds;
 }
 
 static hfx_options job_options(const hfx_scf_options* o)
@@ -289,8 +306,8 @@ hfx_status hfx_rhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, con
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
         double fock_ms = 0.0;
-        GBuilder g = [&](const double* P, double* G, bool) {
-            job.fock_rhf(P, G);
+        GBuilder g = [&](const double* P, double* G, int mode) {
+            job.fock_rhf_ex(P, G, mode == BUILD_DEFAULT && job.mixed(), mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
             fock_ms += job.stats.ms;
         };
         ScfOutput out = rhf_diis(b, o, P0, g);
@@ -315,8 +332,9 @@ hfx_status hfx_uhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, int
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
         double fock_ms = 0.0;
-        JKBuilder jk = [&](const double* a, const double* bb, double* J, double* Ka, double* Kb, bool) {
-            job.fock_uhf(a, bb, J, Ka, Kb);
+        JKBuilder jk = [&](const double* a, const double* bb, double* J, double* Ka, double* Kb, int mode) {
+            job.fock_uhf_ex(a, bb, J, Ka, Kb, mode == BUILD_DEFAULT && job.mixed(),
+                            mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
             fock_ms += job.stats.ms;
         };
         ScfOutput out = uhf_diis(b, o, n_alpha, n_beta, Pa0, Pb0, jk);
@@ -348,8 +366,8 @@ hfx_status hfx_job_rhf(hfx_job* job, const hfx_scf_options* opt, const double* P
         const ScfSetup& setup = job_setup(job);
         Job& j = *job->job;
         double fock_ms = 0.0;
-        GBuilder g = [&](const double* P, double* G, bool) {
-            j.fock_rhf(P, G);
+        GBuilder g = [&](const double* P, double* G, int mode) {
+            j.fock_rhf_ex(P, G, mode == BUILD_DEFAULT && j.mixed(), mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
             fock_ms += j.stats.ms;
         };
         ScfOutput out = rhf_diis(j.basis(), setup, o, P0, g);
@@ -372,8 +390,9 @@ hfx_status hfx_job_uhf(hfx_job* job, const hfx_scf_options* opt, int n_alpha, in
         const ScfSetup& setup = job_setup(job);
         Job& j = *job->job;
         double fock_ms = 0.0;
-        JKBuilder jk = [&](const double* a, const double* b, double* J, double* Ka, double* Kb, bool) {
-            j.fock_uhf(a, b, J, Ka, Kb);
+        JKBuilder jk = [&](const double* a, const double* b, double* J, double* Ka, double* Kb, int mode) {
+            j.fock_uhf_ex(a, b, J, Ka, Kb, mode == BUILD_DEFAULT && j.mixed(),
+                          mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
             fock_ms += j.stats.ms;
         };
         ScfOutput out = uhf_diis(j.basis(), setup, o, n_alpha, n_beta, Pa0, Pb0, jk);
@@ -394,7 +413,7 @@ hfx_status hfx_rhf_diis_with_builder(const hfx_molecule* mol, const hfx_scf_opti
         hfx_scf_options o{};
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
-        GBuilder g = [&](const double* P, double* G, bool) {
+        GBuilder g = [&](const double* P, double* G, int) {
             if (gb(user, P, G) != 0) throw Error(HFX_ERR_INVALID, "caller G builder failed");
         };
         ScfOutput out = rhf_diis(b, o, P0, g);
@@ -413,7 +432,7 @@ hfx_status hfx_uhf_diis_with_builder(const hfx_molecule* mol, const hfx_scf_opti
         hfx_scf_options o{};
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
-        JKBuilder jk = [&](const double* a, const double* bb, double* J, double* Ka, double* Kb, bool) {
+        JKBuilder jk = [&](const double* a, const double* bb, double* J, double* Ka, double* Kb, int) {
             if (jkb(user, a, bb, J, Ka, Kb) != 0) throw Error(HFX_ERR_INVALID, "caller JK builder failed");
         };
         ScfOutput out = uhf_diis(b, o, n_alpha, n_beta, nullptr, nullptr, jk);

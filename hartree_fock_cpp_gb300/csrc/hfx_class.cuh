@@ -1,7 +1,7 @@
 // hfx_class.cuh -- thread-per-shell-quartet kernels for the small
 // angular-momentum classes (at most 36 Cartesian integrals per shell quartet
 // and total L <= 4: (ss|ss) (ps|ss) (ps|ps) (pp|ss) (pp|ps) (ds|ss) (ds|ps)
-// (ds|ds) (dp|ss) (dd|ss)), instantiated for T = double and T = float.
+// (ds|ds) (dp|ss)), instantiated for T = double and T = float.
 //
 // These classes carry most of the primitive quartets of contracted basis sets
 // (cc-pVDZ carbon s shells have 9 primitives, so one (ss|ss) shell quartet is
@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     const Task tk = a.tasks[task];
     const DPair bra = a.pairs[tk.bra];
     const DPair ket = a.pairs[tk.ket];
+    if (density_negligible(bra, ket, a.Dsh, a.dthr)) return;
 
     T acc[NAB][NCD];
 #pragma unroll
@@ -187,7 +188,8 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
 
     const T* __restrict__ recb = a.rec + bra.rec_off;
     const T* __restrict__ reck = a.rec + ket.rec_off;
-    for (int ij = 0; ij < bra.npp; ++ij) {
+    const int ij1 = tk.ij >> 16;
+    for (int ij = tk.ij & 0xffff; ij < ij1; ++ij) {
         const T* rb = recb + ij * SB;
         const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
         const T* cb = rb + 4;

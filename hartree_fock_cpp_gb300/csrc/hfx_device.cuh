@@ -48,8 +48,15 @@ struct __align__(16) DPair {
     double qmax;       // max_ab sqrt((ab|ab)) over the pair's BF pairs
     long long rec_off; // offset of the first primitive-pair record (elements)
     int pc;            // pair class l0*(l0+1)/2 + l1
+    int sh0, sh1;      // shell indices of shell 0 / shell 1 (reference order)
     int pad;
 };
+
+// Triangular index of a shell pair (the pair array's order).
+__host__ __device__ inline int shell_pair_id(int a, int b)
+{
+    return a > b ? a * (a + 1) / 2 + b : b * (b + 1) / 2 + a;
+}
 
 // Primitive-pair record of the class kernels, for a pair of class (l0, l1):
 //   [p, Px, Py, Pz, c_0 ... c_{ncoef-1}] padded to an even length, where the
@@ -82,8 +89,14 @@ __host__ __device__ inline int herm_index(int t, int u, int v)
 
 enum DigestMode { MODE_JK = 0, MODE_ERI = 1, MODE_SCHWARZ = 2 };
 
+// One unit of work: a shell quartet (bra pair, ket pair), restricted to the
+// bra primitive pairs [ij & 0xffff, ij >> 16).  Heavily contracted quartets
+// are split into several such chunks, each digested on its own (J and K are
+// linear in the integrals), so that no thread or warp carries a
+// disproportionate share of a launch.
 struct Task {
     int bra, ket;
+    int ij;
 };
 
 // Work-list descriptor of one launch.
@@ -132,6 +145,8 @@ struct SmallArgs {
     double* J;
     double* Kx;
     double* Kx2;
+    const double* Dsh;         // per shell pair max |D| (density screening), or null
+    double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
 };
 
 // Arguments of the warp-per-shell-quartet kernel.
@@ -158,6 +173,23 @@ struct WarpArgs {
     double* Kx2;
     int slice;                 // per-warp shared-memory slice, in T elements
     int lane_r;                // 1: lane-parallel R allowed for this launch
+    const double* Dsh;         // per shell pair max |D| (density screening), or null
+    double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
 };
+
+#ifdef __CUDACC__
+// Density-weighted Schwarz test of a quartet: the largest density block its
+// J and K contributions touch (AB, CD, AC, AD, BC, BD) times Q_AB Q_CD.
+__device__ __forceinline__ bool density_negligible(const DPair& b, const DPair& k, const double* Dsh, double dthr)
+{
+    if (dthr <= 0.0) return false;
+    double d = fmax(Dsh[b.id], Dsh[k.id]);
+    d = fmax(d, Dsh[shell_pair_id(b.sh0, k.sh0)]);
+    d = fmax(d, Dsh[shell_pair_id(b.sh0, k.sh1)]);
+    d = fmax(d, Dsh[shell_pair_id(b.sh1, k.sh0)]);
+    d = fmax(d, Dsh[shell_pair_id(b.sh1, k.sh1)]);
+    return b.qmax * k.qmax * d < dthr;
+}
+#endif
 
 }  // namespace hfx

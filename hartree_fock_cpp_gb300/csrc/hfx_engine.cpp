@@ -32,6 +32,9 @@ void cuda_check(cudaError_t e, const char* what)
     }
 }
 
+// primitive quartets per thread-level chunk of a shell quartet
+constexpr long long kChunkPrims = 256;
+
 static double flops_per_prim(int la, int lb, int lc, int ld)
 {
     // algorithmic MD flop count per primitive quartet (boys + R + ket + bra + prefactor)
@@ -81,8 +84,13 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
 
     build_pairs();
     compute_schwarz();
-    std::vector<Task> tasks;
-    build_jk_groups();
+    // shell-pair Schwarz maxima into the device pair records (density screening)
+    for (size_t p = 0; p < dpairs_host_.size(); ++p) dpairs_host_[p].qmax = qsh_[p];
+    d_pairs_.upload(dpairs_host_, stream_);
+    d_dsh_.alloc(std::max<size_t>(1, dpairs_host_.size()));
+    build_jk_groups(false, gs_fp64_);
+    if (mixed()) build_jk_groups(true, gs_mixed_);
+    d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
     cuda_check(cudaStreamSynchronize(stream_), "job setup");
 }
 
@@ -102,7 +110,7 @@ Job::~Job()
 
 bool is_small_class(int pcb, int pck)
 {
-    static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0}, {5, 0}};
+    static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0}};
     for (auto& c : small)
         if (c[0] == pcb && c[1] == pck) return true;
     return false;
@@ -225,6 +233,8 @@ PairData build_pair_data(const Basis& basis)
             d.qmax = 0.0;
             d.rec_off = rec_off;
             d.pc = pc;
+            d.sh0 = s0;
+            d.sh1 = s1;
             pd.dpairs.push_back(d);
             pd.hpairs.push_back(hp);
         }
@@ -235,6 +245,7 @@ void Job::build_pairs()
 {
     PairData pd = build_pair_data(basis_);
     hpairs_ = std::move(pd.hpairs);
+    dpairs_host_ = pd.dpairs;
     d_pairs_.upload(pd.dpairs, stream_);
     d_ppgeo_.upload(pd.geo, stream_);
     d_epool_.upload(pd.epool, stream_);
@@ -282,7 +293,7 @@ void Job::compute_schwarz()
     std::vector<Task> t(np);
     int maxacc = 0, maxw = 0, maxr = 0;
     for (int p = 0; p < np; ++p) {
-        t[p] = {p, p};
+        t[p] = {p, p, hpairs_[p].npp << 16};
         int L = hpairs_[p].l0 + hpairs_[p].l1;
         int nab = ncart(hpairs_[p].l0) * ncart(hpairs_[p].l1);
         maxacc = std::max(maxacc, nab * nab);
@@ -332,7 +343,7 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
             if (thr >= 0.0 && qsh_[X] * qsh_[Y] < thr) continue;
             int bra = X, ket = Y;
             if (key(Y) > key(X)) std::swap(bra, ket);
-            tasks.push_back({bra, ket});
+            tasks.push_back({bra, ket, hpairs_[bra].npp << 16});
         }
     std::vector<double> c(tasks.size());
     double fsum = 0.0, psum = 0.0;
@@ -358,10 +369,9 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     tasks.swap(sorted);
 }
 
-void Job::build_jk_groups()
+void Job::build_jk_groups(bool mixed, GroupSet& gs)
 {
     const double thr = opt_.screening_threshold;
-    const bool mixed = opt_.precision == HFX_PREC_MIXED;
     const double tau = opt_.fp32_threshold;
     const int np = (int)hpairs_.size();
     auto pcof = [&](int p) { return pair_class(hpairs_[p].l0, hpairs_[p].l1); };
@@ -380,17 +390,25 @@ void Job::build_jk_groups()
             const bool f32 = mixed && bound < tau;
             const HostPair& b = hpairs_[bra];
             const HostPair& k = hpairs_[ket];
-            const double c = (double)b.npp * k.npp * flops_per_prim(b.l0, b.l1, k.l0, k.l1);
+            const double fpp = flops_per_prim(b.l0, b.l1, k.l0, k.l1);
             const int pcb = pcof(bra), pck = pcof(ket);
-            Bucket& bk = is_small_class(pcb, pck) ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
-            bk.t.push_back({bra, ket});
-            bk.cost.push_back(c);
+            const bool sm = is_small_class(pcb, pck);
+            Bucket& bk = sm ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
+            // split the bra primitive pairs so that a chunk holds at most
+            // kChunkPrims primitive quartets (per thread) or 16x that (per warp)
+            const long long cap = sm ? kChunkPrims : 16LL * kChunkPrims;
+            const long long pq = (long long)b.npp * k.npp;
+            const int nch = (int)std::min<long long>(b.npp, std::max<long long>(1, (pq + cap - 1) / cap));
+            for (int c = 0; c < nch; ++c) {
+                const int i0 = (int)((long long)b.npp * c / nch), i1 = (int)((long long)b.npp * (c + 1) / nch);
+                bk.t.push_back({bra, ket, i0 | (i1 << 16)});
+                bk.cost.push_back((double)(i1 - i0) * k.npp * fpp);
+            }
         }
     std::vector<Task> all;
-    groups_.clear();
-    flops_ = flops32_ = prim_quartets_ = 0.0;
-    quartets32_ = 0.0;
-    ntasks_ = 0;
+    std::vector<LaunchGroup>& groups = gs.groups;
+    groups.clear();
+    gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
     auto sorted = [](Bucket& bk) {
         std::vector<size_t> idx(bk.t.size());
         std::iota(idx.begin(), idx.end(), 0);
@@ -412,9 +430,9 @@ void Job::build_jk_groups()
                 for (size_t i : sorted(bk)) {
                     all.push_back(bk.t[i]);
                     g.flops += bk.cost[i];
-                    g.prims += (double)hpairs_[bk.t[i].bra].npp * hpairs_[bk.t[i].ket].npp;
+                    g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * hpairs_[bk.t[i].ket].npp;
                 }
-                groups_.push_back(g);
+                groups.push_back(g);
             }
     const size_t elem[2] = {sizeof(double), sizeof(float)};
     for (int f = 0; f < 2; ++f) {
@@ -443,7 +461,7 @@ void Job::build_jk_groups()
                 slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true));
                 all.push_back(bk.t[i]);
                 g.flops += bk.cost[i];
-                g.prims += (double)b.npp * k.npp;
+                g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * k.npp;
             }
             g.slice = (slice + 1) & ~1;
             g.warps_per_cta = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - 8064) / (g.slice * elem[f])));
@@ -451,34 +469,46 @@ void Job::build_jk_groups()
             int ctas_per_sm = (int)std::max<size_t>(1, (228 * 1024) / (sm + 1024));
             long long need = ((long long)g.n + g.warps_per_cta - 1) / g.warps_per_cta;
             g.grid = (int)std::min<long long>(need, (long long)nsm_ * ctas_per_sm);
-            groups_.push_back(g);
+            groups.push_back(g);
         }
     }
-    for (const auto& g : groups_) {
+    for (const auto& g : groups) {
         if (g.fp32) {
-            flops32_ += g.flops;
-            quartets32_ += (double)g.n;
+            gs.flops32 += g.flops;
+            for (size_t i = g.off; i < g.off + g.n; ++i)
+                if ((all[i].ij & 0xffff) == 0) gs.quartets32 += 1.0;
         } else {
-            flops_ += g.flops;
+            gs.flops64 += g.flops;
         }
-        prim_quartets_ += g.prims;
+        gs.prims += g.prims;
     }
-    ntasks_ = (int)all.size();
-    d_jk_tasks_.upload(all, stream_);
-    d_counters_.alloc(std::max<size_t>(1, groups_.size()));
+    gs.ntasks = (int)all.size();
+    gs.nquartets = 0;
+    for (const auto& t : all)
+        if ((t.ij & 0xffff) == 0) ++gs.nquartets;
+    gs.tasks.upload(all, stream_);
 }
 
 void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
-                    double* Kx2, int* counters)
+                    double* Kx2, int* counters, bool mixed_plan, double dthr)
 {
+    const GroupSet& gs = plan(mixed_plan);
+    const std::vector<LaunchGroup>& groups = gs.groups;
+    const Task* tasks = gs.tasks.p;
+    const double* Dsh = nullptr;
+    if (dthr > 0.0) {
+        cuda_check(launch_density_blocks(d_pairs_.p, (int)dpairs_host_.size(), Dk, Dk2, basis_.K, d_dsh_.p, stream_),
+                   "density blocks");
+        Dsh = d_dsh_.p;
+    }
     int* ctr = counters ? counters : d_counters_.p;
-    cuda_check(cudaMemsetAsync(ctr, 0, sizeof(int) * d_counters_.n, stream_), "memset counters");
+    cuda_check(cudaMemsetAsync(ctr, 0, sizeof(int) * std::max<size_t>(1, groups.size()), stream_), "memset counters");
     cuda_check(cudaEventRecord(fork_ev_, stream_), "fork");
     for (auto st : aux_) cuda_check(cudaStreamWaitEvent(st, fork_ev_, 0), "fork wait");
     // warp groups (the long ones) on the main stream, small classes spread over the others
     int next_aux = 0;
-    for (size_t gi = 0; gi < groups_.size(); ++gi) {
-        const LaunchGroup& g = groups_[gi];
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        const LaunchGroup& g = groups[gi];
         if (g.n == 0) continue;
         cudaStream_t st = stream_;
         if (g.kind == 0) {
@@ -488,24 +518,26 @@ void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk
         cudaError_t e;
         if (g.kind == 0) {
             if (g.fp32) {
-                SmallArgs<float> a{d_pairs_.p, d_rec32_.p, d_jk_tasks_.p + g.off, (int)g.n, d_boys32_.p,
-                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2};
+                SmallArgs<float> a{d_pairs_.p, d_rec32_.p, tasks + g.off, (int)g.n, d_boys32_.p,
+                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
                 e = launch_small_f32(g.pcb, g.pck, &a, nk, st);
             } else {
-                SmallArgs<double> a{d_pairs_.p, d_rec64_.p, d_jk_tasks_.p + g.off, (int)g.n, d_boys_.p,
-                                    opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2};
+                SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys_.p,
+                                    opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
                 e = launch_small_f64(g.pcb, g.pck, &a, nk, st);
             }
         } else {
             if (g.fp32) {
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
-                                  d_jk_tasks_.p + g.off, (int)g.n, ctr + gi, d_boys32_.p,
-                                  opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
+                                  tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
+                                  opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                  Dsh, dthr};
                 e = launch_warp(true, &a, nk, g.grid, g.warps_per_cta, st);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
-                                   d_jk_tasks_.p + g.off, (int)g.n, ctr + gi, d_boys_.p,
-                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1};
+                                   tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
+                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                   Dsh, dthr};
                 e = launch_warp(false, &a, nk, g.grid, g.warps_per_cta, st);
             }
         }
@@ -517,22 +549,26 @@ void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk
     }
 }
 
-void Job::record_stats(int launches)
+void Job::record_stats(int launches) { record_stats_plan(launches, plan(mixed())); }
+
+void Job::record_stats_plan(int launches, const GroupSet& gs)
 {
     float ms = 0.f, kms = 0.f;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
     cudaEventElapsedTime(&kms, evk0_, evk1_);
     stats.ms = ms;
     stats.kernel_ms = kms;
-    stats.quartets = ntasks_;
-    stats.quartets_fp32 = quartets32_;
-    stats.prim_quartets = prim_quartets_;
-    stats.flops_fp64 = flops_;
-    stats.flops_fp32 = flops32_;
+    stats.quartets = gs.nquartets;
+    stats.quartets_fp32 = gs.quartets32;
+    stats.prim_quartets = gs.prims;
+    stats.flops_fp64 = gs.flops64;
+    stats.flops_fp32 = gs.flops32;
     stats.launches = launches;
 }
 
-void Job::fock_rhf_device(const double* dP, double* dG)
+void Job::fock_rhf_device(const double* dP, double* dG) { fock_rhf_device_ex(dP, dG, mixed(), 0.0); }
+
+void Job::fock_rhf_device_ex(const double* dP, double* dG, bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     int K = basis_.K;
@@ -543,12 +579,12 @@ void Job::fock_rhf_device(const double* dP, double* dG)
     cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr);
+    launch_jk(1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr, nullptr, mixed_plan, dthr);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    record_stats((int)groups_.size() + 1);
+    record_stats_plan((int)plan(mixed_plan).groups.size() + 1, plan(mixed_plan));
 }
 
 void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, double* Kacc, int* counters)
@@ -560,15 +596,65 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
     cuda_check(cudaMemsetAsync(Jacc, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(Kacc, 0, n * sizeof(double), stream_), "memset");
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters);
+    launch_jk(1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters, mixed(), 0.0);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_rhf(Jacc, Kacc, dG, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    record_stats((int)groups_.size() + 1);
+    record_stats((int)plan(mixed()).groups.size() + 1);
+}
+
+double Job::autotune_fp32_threshold(const double* P, double target_dE, double* dE_out, double* ms64, double* msmx)
+{
+    const int K = basis_.K;
+    const size_t n = (size_t)K * K;
+    std::vector<double> G64(n), Gm(n);
+    fock_rhf_ex(P, G64.data(), false, 0.0);
+    fock_rhf_ex(P, G64.data(), false, 0.0);
+    const double t64 = stats.ms;
+    static const double cand[] = {3e-1, 1e-1, 3e-2, 1e-2, 3e-3, 1e-3, 1e-4, 1e-5};
+    double best = 0.0, best_dE = 0.0, best_ms = t64;
+    const int prec0 = opt_.precision;
+    const double tau0 = opt_.fp32_threshold;
+    opt_.precision = HFX_PREC_MIXED;
+    for (double tau : cand) {
+        opt_.fp32_threshold = tau;
+        build_jk_groups(true, gs_mixed_);
+        d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
+        fock_rhf_ex(P, Gm.data(), true, 0.0);
+        double dE = 0.0;
+        for (size_t i = 0; i < n; ++i) dE += P[i] * (Gm[i] - G64[i]);
+        dE *= 0.5;
+        if (std::fabs(dE) <= target_dE) {
+            fock_rhf_ex(P, Gm.data(), true, 0.0);
+            best = tau;
+            best_dE = dE;
+            best_ms = stats.ms;
+            break;
+        }
+    }
+    if (best > 0.0) {
+        opt_.fp32_threshold = best;
+        build_jk_groups(true, gs_mixed_);
+    } else {
+        opt_.precision = prec0;
+        opt_.fp32_threshold = tau0;
+        if (mixed()) build_jk_groups(true, gs_mixed_);
+    }
+    d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
+    if (dE_out) *dE_out = best_dE;
+    if (ms64) *ms64 = t64;
+    if (msmx) *msmx = best_ms;
+    return best;
 }
 
 void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb)
+{
+    fock_uhf_device_ex(dPa, dPb, dJ, dKa, dKb, mixed(), 0.0);
+}
+
+void Job::fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb,
+                             bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     int K = basis_.K;
@@ -583,27 +669,35 @@ void Job::fock_uhf_device(const double* dPa, const double* dPb, double* dJ, doub
     cuda_check(cudaMemsetAsync(d_K2_.p, 0, n * sizeof(double), stream_), "memset");
     cuda_check(launch_add(dPa, dPb, d_Dj_.p, (int)n, stream_), "add");
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(2, d_Dj_.p, dPa, dPb, d_J_.p, d_K_.p, d_K2_.p);
+    launch_jk(2, d_Dj_.p, dPa, dPb, d_J_.p, d_K_.p, d_K2_.p, nullptr, mixed_plan, dthr);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
     cuda_check(launch_finish_uhf(d_J_.p, d_K_.p, d_K2_.p, dJ, dKa, dKb, K, stream_), "finish");
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
-    record_stats((int)groups_.size() + 2);
+    record_stats_plan((int)plan(mixed_plan).groups.size() + 2, plan(mixed_plan));
 }
 
-void Job::fock_rhf(const double* P, double* G)
+void Job::fock_rhf(const double* P, double* G) { fock_rhf_ex(P, G, mixed(), 0.0); }
+
+void Job::fock_rhf_ex(const double* P, double* G, bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     size_t n = (size_t)basis_.K * basis_.K;
     d_D_.alloc(n);
     d_out1_.alloc(n);
     cuda_check(cudaMemcpyAsync(d_D_.p, P, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
-    fock_rhf_device(d_D_.p, d_out1_.p);
+    fock_rhf_device_ex(d_D_.p, d_out1_.p, mixed_plan, dthr);
     cuda_check(cudaMemcpyAsync(G, d_out1_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
     cuda_check(cudaStreamSynchronize(stream_), "D2H");
 }
 
 void Job::fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb)
+{
+    fock_uhf_ex(Pa, Pb, J, Ka, Kb, mixed(), 0.0);
+}
+
+void Job::fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, bool mixed_plan,
+                      double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     size_t n = (size_t)basis_.K * basis_.K;
@@ -614,7 +708,7 @@ void Job::fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, do
     d_out3_.alloc(n);
     cuda_check(cudaMemcpyAsync(d_D_.p, Pa, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
     cuda_check(cudaMemcpyAsync(d_D2_.p, Pb, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
-    fock_uhf_device(d_D_.p, d_D2_.p, d_out1_.p, d_out2_.p, d_out3_.p);
+    fock_uhf_device_ex(d_D_.p, d_D2_.p, d_out1_.p, d_out2_.p, d_out3_.p, mixed_plan, dthr);
     cuda_check(cudaMemcpyAsync(J, d_out1_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
     cuda_check(cudaMemcpyAsync(Ka, d_out2_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
     cuda_check(cudaMemcpyAsync(Kb, d_out3_.p, n * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");

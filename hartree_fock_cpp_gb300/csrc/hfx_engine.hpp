@@ -23,6 +23,8 @@ cudaError_t launch_small_f64(int pcb, int pck, const void* args, int nk, cudaStr
 cudaError_t launch_small_f32(int pcb, int pck, const void* args, int nk, cudaStream_t st);
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
 int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
+cudaError_t launch_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
+                                  double* Dsh, cudaStream_t st);
 bool is_small_class(int pcb, int pck);
 
 void cuda_check(cudaError_t e, const char* what);
@@ -101,6 +103,14 @@ struct LaunchGroup {
 };
 PairData build_pair_data(const Basis& b);
 
+// The launch plan of one precision mode.
+struct GroupSet {
+    std::vector<LaunchGroup> groups;
+    DevBuf<Task> tasks;
+    int ntasks = 0, nquartets = 0;
+    double flops64 = 0.0, flops32 = 0.0, prims = 0.0, quartets32 = 0.0;
+};
+
 class Job {
 public:
     Job(Basis b, const hfx_options& opt);
@@ -113,11 +123,27 @@ public:
     void schwarz_host(std::vector<double>& Qbf) const;
     // device-pointer Fock builds (synchronous)
     void fock_rhf_device(const double* dP, double* dG);
+    // Builds with an explicit precision plan (mixed = false: every quartet in
+    // FP64) and density-weighted screening threshold (0: none; used by the
+    // incremental builds of the mixed-precision SCF).
+    void fock_rhf_device_ex(const double* dP, double* dG, bool mixed, double dthr);
+    void fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb, bool mixed,
+                            double dthr);
+    void fock_rhf_ex(const double* P, double* G, bool mixed, double dthr);
+    void fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, bool mixed, double dthr);
+    bool mixed() const { return opt_.precision == HFX_PREC_MIXED; }
+    double fp32_threshold() const { return opt_.fp32_threshold; }
+    // Pick the FP32 threshold: for each candidate (largest first) build G in
+    // mixed precision at density P and keep the largest tau whose energy
+    // change 1/2 sum P (G_tau - G_fp64) stays within target_dE; the job is
+    // switched to mixed precision at that tau.  Returns tau (0 if none fits).
+    double autotune_fp32_threshold(const double* P, double target_dE, double* dE_out, double* ms_fp64,
+                                   double* ms_mixed);
     // RHF build whose scratch (J/K accumulators, work-queue counters) is
     // supplied by the caller; allocates nothing.  Jacc/Kacc hold K*K doubles,
     // counters num_launch_groups() ints.
     void fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, double* Kacc, int* counters);
-    int num_launch_groups() const { return (int)groups_.size(); }
+    int num_launch_groups() const { return (int)plan(true).groups.size(); }
     void fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb);
     void fock_rhf(const double* P, double* G);
     void fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb);
@@ -143,14 +169,17 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evk0_ = nullptr, evk1_ = nullptr;
 
-    void build_jk_groups();
+    void build_jk_groups(bool mixed, GroupSet& gs);
     void launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
-                   double* Kx2, int* counters = nullptr);
+                   double* Kx2, int* counters = nullptr, bool mixed_plan = false, double dthr = 0.0);
+    const GroupSet& plan(bool mixed_plan) const { return mixed_plan && mixed() ? gs_mixed_ : gs_fp64_; }
+    void record_stats_plan(int launches, const GroupSet& gs);
 
     std::vector<HostPair> hpairs_;
-    std::vector<LaunchGroup> groups_;
-    DevBuf<Task> d_jk_tasks_;
+    GroupSet gs_fp64_, gs_mixed_;
     DevBuf<int> d_counters_;
+    DevBuf<double> d_dsh_;
+    std::vector<DPair> dpairs_host_;
     DevBuf<double> d_rec64_;
     DevBuf<float> d_rec32_;
     DevBuf<float> d_boys32_;
@@ -171,6 +200,7 @@ private:
     DevBuf<unsigned long long> d_qsh_;
     DevBuf<Task> d_tasks_;
     int ntasks_ = 0;
+    int nquartets_ = 0;
     int maxacc_ = 0, maxw_ = 0, maxr_ = 0;
     DevBuf<int> d_counter_;
     DevBuf<double> d_D_, d_D2_, d_Dj_, d_J_, d_K_, d_K2_, d_out1_, d_out2_, d_out3_;

@@ -282,6 +282,33 @@ __global__ void k_add(const double* A, const double* B, double* C, int n)
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) C[e] = A[e] + B[e];
 }
 
+// Dsh[p] = max over the (A, B) block of max(|D1|, |D2|), for every shell pair
+// p (D2 may be null); the density-weighted screening of incremental builds.
+__global__ void k_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
+                                 double* Dsh)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const DPair pr = pairs[p];
+    const int n0 = dncart(pr.l0), n1 = dncart(pr.l1);
+    double m = 0.0;
+    for (int a = 0; a < n0; ++a)
+        for (int b = 0; b < n1; ++b) {
+            long long e = (long long)(pr.bf0 + a) * K + pr.bf1 + b;
+            m = fmax(m, fabs(D1[e]));
+            if (D2) m = fmax(m, fabs(D2[e]));
+        }
+    Dsh[p] = m;
+}
+
+cudaError_t launch_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
+                                  double* Dsh, cudaStream_t st)
+{
+    if (npairs == 0) return cudaSuccess;
+    k_density_blocks<<<(npairs + 127) / 128, 128, 0, st>>>(pairs, npairs, D1, D2, K, Dsh);
+    return cudaGetLastError();
+}
+
 // Host-side launch helpers (called from hfx_engine.cpp).
 size_t generic_smem_bytes(int maxacc, int maxw, int maxr)
 {

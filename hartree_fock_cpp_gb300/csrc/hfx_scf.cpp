@@ -184,11 +184,49 @@ ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
     out.n_electrons = n_e;
     out.E_nuc = E_nuc;
     std::vector<double> G(K * K), C, e;
+    // Mixed precision: FP32/FP64 builds until the density settles, then one
+    // full FP64 build and FP64 builds of the density change from there on
+    // (G_n = G_{n-1} + G[P_n - P_{n-1}]), so the converged energy carries FP64
+    // accuracy while most builds run mostly in FP32.
+    const bool mixed = opt.precision == HFX_PREC_MIXED;
+    int phase = mixed ? 0 : 2;          // 0 mixed, 1 next build full FP64, 2 plain / incremental FP64
+    bool have_ref = false;
+    std::vector<double> G_ref, P_ref, dP(K * K), dG(K * K);
+    auto build = [&](const std::vector<double>& Pm, std::vector<double>& Gm) {
+        ++out.fock_builds;
+        if (!mixed) {
+            gbuild(Pm.data(), Gm.data(), BUILD_DEFAULT);
+            ++out.fp64_builds;
+            return;
+        }
+        if (phase == 0) {
+            gbuild(Pm.data(), Gm.data(), BUILD_DEFAULT);
+            ++out.mixed_builds;
+            return;
+        }
+        if (phase == 1 || !have_ref || opt.fp64_final_cycles < 0) {
+            gbuild(Pm.data(), Gm.data(), BUILD_FP64);
+            ++out.fp64_builds;
+            if (opt.fp64_final_cycles >= 0) {
+                G_ref = Gm;
+                P_ref = Pm;
+                have_ref = true;
+                phase = 2;
+            }
+            return;
+        }
+        for (int i = 0; i < K * K; ++i) dP[i] = Pm[i] - P_ref[i];
+        gbuild(dP.data(), dG.data(), BUILD_FP64_DELTA);
+        ++out.delta_builds;
+        for (int i = 0; i < K * K; ++i) Gm[i] = G_ref[i] + dG[i];
+        G_ref = Gm;
+        P_ref = Pm;
+    };
+    const double switch_tol = 10.0 * opt.epsilon;
     int n_it = 0;
     for (int it = 0; it < opt.max_iterations; ++it) {
         ++n_it;
-        gbuild(P.data(), G.data(), false);
-        ++out.fock_builds;
+        build(P, G);
         std::vector<double> F(K * K);
         for (int i = 0; i < K * K; ++i) F[i] = H[i] + G[i];
         if (!finite_all(F)) throw Error(HFX_ERR_NUMERIC, "non-finite Fock matrix");
@@ -204,10 +242,10 @@ ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
         bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - out.E_prev) < opt.energy_threshold);
         out.E_prev = E_cur;
         out.last_rmsd = Pd;
-        if (Pd < opt.epsilon && en < opt.epsilon && dE_ok) {
+        if (phase == 0 && Pd < switch_tol) phase = 1;
+        if (Pd < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
             // rhf_final_check (scf.hpp:107-137)
-            gbuild(Pn.data(), G.data(), true);
-            ++out.fock_builds;
+            build(Pn, G);
             std::vector<double> Ff(K * K);
             for (int i = 0; i < K * K; ++i) Ff[i] = H[i] + G[i];
             double fe = norm2(error_matrix(K, Pn, Ff, S));
@@ -225,8 +263,8 @@ ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
             for (int i = 0; i < K * K; ++i) P[i] = opt.damping * Pn[i] + (1 - opt.damping) * P[i];
         }
         if (it == opt.max_iterations - 1) {
-            gbuild(P.data(), G.data(), true);
-            ++out.fock_builds;
+            if (phase == 0) phase = 1;
+            build(P, G);
             std::vector<double> Ff(K * K);
             for (int i = 0; i < K * K; ++i) Ff[i] = H[i] + G[i];
             out.E_ele = energy(P, Ff, H);
@@ -265,11 +303,58 @@ ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
     out.n_electrons = n_e;
     out.E_nuc = E_nuc;
     std::vector<double> J(K * K), Ka(K * K), Kb(K * K), Ca, Cb, Ea, Eb;
+    const bool mixed = opt.precision == HFX_PREC_MIXED;
+    int phase = mixed ? 0 : 2;
+    bool have_ref = false;
+    std::vector<double> Jr, Kar, Kbr, Par, Pbr, dPa(K * K), dPb(K * K), dJ(K * K), dKa(K * K), dKb(K * K);
+    auto build = [&](const std::vector<double>& A, const std::vector<double>& B) {
+        ++out.fock_builds;
+        if (!mixed) {
+            jk(A.data(), B.data(), J.data(), Ka.data(), Kb.data(), BUILD_DEFAULT);
+            ++out.fp64_builds;
+            return;
+        }
+        if (phase == 0) {
+            jk(A.data(), B.data(), J.data(), Ka.data(), Kb.data(), BUILD_DEFAULT);
+            ++out.mixed_builds;
+            return;
+        }
+        if (phase == 1 || !have_ref || opt.fp64_final_cycles < 0) {
+            jk(A.data(), B.data(), J.data(), Ka.data(), Kb.data(), BUILD_FP64);
+            ++out.fp64_builds;
+            if (opt.fp64_final_cycles >= 0) {
+                Jr = J;
+                Kar = Ka;
+                Kbr = Kb;
+                Par = A;
+                Pbr = B;
+                have_ref = true;
+                phase = 2;
+            }
+            return;
+        }
+        for (int i = 0; i < K * K; ++i) {
+            dPa[i] = A[i] - Par[i];
+            dPb[i] = B[i] - Pbr[i];
+        }
+        jk(dPa.data(), dPb.data(), dJ.data(), dKa.data(), dKb.data(), BUILD_FP64_DELTA);
+        ++out.delta_builds;
+        for (int i = 0; i < K * K; ++i) {
+            J[i] = Jr[i] + dJ[i];
+            Ka[i] = Kar[i] + dKa[i];
+            Kb[i] = Kbr[i] + dKb[i];
+        }
+        Jr = J;
+        Kar = Ka;
+        Kbr = Kb;
+        Par = A;
+        Pbr = B;
+    };
+    const double switch_tol = 10.0 * opt.epsilon;
     int n_it = 0;
     for (int it = 0; it < opt.max_iterations; ++it) {
         ++n_it;
-        jk(Pa.data(), Pb.data(), J.data(), Ka.data(), Kb.data(), false);
-        ++out.fock_builds;
+        build(Pa, Pb);
         std::vector<double> Fa(K * K), Fb(K * K);
         for (int i = 0; i < K * K; ++i) {
             Fa[i] = H[i] + J[i] - Ka[i];
@@ -295,10 +380,10 @@ ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
         bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - out.E_prev) < opt.energy_threshold);
         out.E_prev = E_cur;
         out.last_rmsd = std::max(da, db);
-        if (da < opt.epsilon && db < opt.epsilon && en < opt.epsilon && dE_ok) {
+        if (phase == 0 && std::max(da, db) < switch_tol) phase = 1;
+        if (da < opt.epsilon && db < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
             // uhf_final_check (scf.hpp:140-185)
-            jk(Pan.data(), Pbn.data(), J.data(), Ka.data(), Kb.data(), true);
-            ++out.fock_builds;
+            build(Pan, Pbn);
             std::vector<double> Faf(K * K), Fbf(K * K);
             for (int i = 0; i < K * K; ++i) {
                 Faf[i] = H[i] + J[i] - Ka[i];
@@ -324,8 +409,8 @@ ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
             }
         }
         if (it == opt.max_iterations - 1) {
-            jk(Pa.data(), Pb.data(), J.data(), Ka.data(), Kb.data(), true);
-            ++out.fock_builds;
+            if (phase == 0) phase = 1;
+            build(Pa, Pb);
             double E = 0.0;
             std::vector<double> Faf(K * K), Fbf(K * K);
             for (int i = 0; i < K * K; ++i) {

@@ -8,10 +8,16 @@
 
 namespace hfx {
 
-// G builder: P -> G = J[P] - 1/2 K[P]; `final` marks the final-check build.
-using GBuilder = std::function<void(const double* P, double* G, bool final)>;
+// Build modes requested by the drivers.
+enum BuildMode {
+    BUILD_DEFAULT = 0,      // the job's own precision plan (FP64, or mixed FP32/FP64)
+    BUILD_FP64 = 1,         // every quartet in FP64
+    BUILD_FP64_DELTA = 2    // FP64 build of a density difference, density-weighted screening
+};
+// G builder: P -> G = J[P] - 1/2 K[P] (linear in P).
+using GBuilder = std::function<void(const double* P, double* G, int mode)>;
 // UHF builder: (Pa, Pb) -> J[Pa+Pb], K[Pa], K[Pb].
-using JKBuilder = std::function<void(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, bool final)>;
+using JKBuilder = std::function<void(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, int mode)>;
 
 struct ScfOutput {
     double E_tot = 0, E_ele = 0, E_nuc = 0, E_prev = 0, last_rmsd = 0;
@@ -19,6 +25,7 @@ struct ScfOutput {
     bool converged = false;
     int K = 0, n_electrons = 0;
     int fock_builds = 0;
+    int mixed_builds = 0, fp64_builds = 0, delta_builds = 0;
     double seconds = 0;
     std::vector<double> P, P2, C, e, e2;
 };

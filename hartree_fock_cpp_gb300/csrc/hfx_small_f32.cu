@@ -18,7 +18,6 @@ cudaError_t launch_small_f32(int pcb, int pck, const void* args, int nk, cudaStr
     case 3 * 16 + 1: return launch_small<float, 2, 0, 1, 0>(a, nk, st);   // (ds|ps)
     case 3 * 16 + 3: return launch_small<float, 2, 0, 2, 0>(a, nk, st);   // (ds|ds)
     case 4 * 16 + 0: return launch_small<float, 2, 1, 0, 0>(a, nk, st);   // (dp|ss)
-    case 5 * 16 + 0: return launch_small<float, 2, 2, 0, 0>(a, nk, st);   // (dd|ss)
     default: return cudaErrorInvalidValue;
     }
 }

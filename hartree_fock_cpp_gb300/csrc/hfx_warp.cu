@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         const Task task = a.tasks[tk];
         const DPair bra = a.pairs[task.bra];
         const DPair ket = a.pairs[task.ket];
+        if (density_negligible(bra, ket, a.Dsh, a.dthr)) continue;
         const PairClassTab cb = a.pct[bra.pc];
         const PairClassTab ck = a.pct[ket.pc];
         const int L1 = bra.l0 + bra.l1, L2 = ket.l0 + ket.l1, L = L1 + L2;
@@ -219,7 +220,8 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         T* Sd = Ra + (lane_mode ? HL * 32 : 2 * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
         for (int e = lane; e < nout; e += 32) acc[e] = (T)0;
 
-        for (int ij = 0; ij < bra.npp; ++ij) {
+        const int ij_end = task.ij >> 16;
+        for (int ij = task.ij & 0xffff; ij < ij_end; ++ij) {
             const T* rb = rec + bra.rec_off + (long long)ij * cb.stride;
             const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
             for (int e = lane; e < nw; e += 32) W[e] = (T)0;

@@ -163,6 +163,16 @@ typedef struct {
 
 hfx_status hfx_last_build_stats(const hfx_job *job, hfx_build_stats *stats);
 
+/* Autotune the mixed-precision cut for this job: at density P (K*K host, e.g.
+ * a converged or near-converged density), build G in FP64 and then in mixed
+ * precision for tau = 0.3, 0.1, 0.03, ... 1e-5, keep the largest tau with
+ * |1/2 sum P (G_tau - G_fp64)| <= target_dE (Eh) and switch the job to mixed
+ * precision at that tau.  tau = 0 if no candidate qualifies (job unchanged).
+ * dE / ms_fp64 / ms_mixed (optional) report the chosen tau's energy change and
+ * the two build times. */
+hfx_status hfx_autotune_fp32_threshold(hfx_job *job, const double *P, double target_dE, double *tau, double *dE,
+                                       double *ms_fp64, double *ms_mixed);
+
 /* ---- SCF drivers (scf.hpp semantics) -------------------------------------- */
 
 typedef struct {
@@ -174,7 +184,8 @@ typedef struct {
     int charge;
     int precision;              /* HFX_PREC_FP64 / HFX_PREC_MIXED */
     double fp32_threshold;      /* mixed precision cut (see hfx_options) */
-    int fp64_final_cycles;      /* mixed: rebuild incrementally in FP64 once RMSD(P) < 1e3*epsilon; default 1 (on) */
+    int fp64_final_cycles;      /* mixed: once RMSD(P) < 10 eps switch to one full FP64 build and FP64
+                                   builds of the density change (default 0 = on; -1: full FP64 builds instead) */
     int start_diis;             /* default 4 (scf.hpp:235) */
     int max_history;            /* default 8 (scf.hpp:236) */
     int verbose;
@@ -190,7 +201,10 @@ typedef struct {
     double seconds;             /* wall time of the whole SCF */
     double fock_ms;             /* summed device time of the Fock builds */
     int fock_builds;
-    int reserved[7];
+    int mixed_builds;           /* builds with FP32 quartets (mixed precision) */
+    int fp64_builds;            /* full FP64 builds */
+    int delta_builds;           /* FP64 builds of a density change (mixed precision, final cycles) */
+    int reserved[4];
 } hfx_scf_result;
 
 /* RHF (scf.hpp:205-419).  P0: optional K*K initial density (NULL = zero).

@@ -140,3 +140,39 @@ def test_device_pointer_build_matches_host_build():
         torch.cuda.synchronize()
         fb.repulsion_matrix_device(dP.data_ptr(), dG.data_ptr())
         assert np.abs(dG.cpu().numpy() - G).max() < 1e-12
+
+
+# ---------------- mixed precision ----------------
+
+@pytest.mark.parametrize("tau", [1e-2, 1e-1])
+def test_mixed_precision_rhf_decane_energy(tau):
+    """FP32 for quartets with Schwarz bound < tau, final cycles as FP64 builds
+    of the density change: |dE| vs the all-FP64 GPU path within 1 uHa."""
+    cfg = W.n_decane()
+    kw = dict(epsilon=1e-7, energy_threshold=1e-8)
+    r64 = H.rhf_diis(cfg, "6-31G*", **kw)
+    rmx = H.rhf_diis(cfg, "6-31G*", precision=H.HFX_PREC_MIXED, fp32_threshold=tau, **kw)
+    assert r64["converged"] and rmx["converged"]
+    assert abs(rmx["E_tot"] - r64["E_tot"]) < E_TOL
+    assert abs(rmx["iterations"] - r64["iterations"]) <= 1
+    assert rmx["mixed_builds"] > 0 and rmx["delta_builds"] > 0
+
+
+def test_mixed_precision_fock_matrix_close_to_fp64():
+    cfg = W.n_decane()
+    P = _sym(194, 7) * 0.05
+    with H.FockBuilder(config=cfg, basis_set="6-31G*") as f64:
+        G64 = f64.repulsion_matrix(P)
+    with H.FockBuilder(config=cfg, basis_set="6-31G*", precision=H.HFX_PREC_MIXED, fp32_threshold=1e-2) as fmx:
+        Gmx = fmx.repulsion_matrix(P)
+        st = fmx.stats()
+    assert st["quartets_fp32"] > 0.3 * st["quartets"]
+    assert np.abs(Gmx - G64).max() < 1e-6
+
+
+def test_mixed_precision_uhf_energy():
+    cfg = [("O", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.83))]
+    r64 = H.uhf_diis(cfg, "cc-pVDZ", spin_occ=(5, 4))
+    rmx = H.uhf_diis(cfg, "cc-pVDZ", spin_occ=(5, 4), precision=H.HFX_PREC_MIXED, fp32_threshold=1e-1)
+    assert r64["converged"] and rmx["converged"]
+    assert abs(rmx["E_tot"] - r64["E_tot"]) < E_TOL
