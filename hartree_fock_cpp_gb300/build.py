@@ -65,7 +65,9 @@ def build(verbose=False, force=False):
             if r.returncode != 0:
                 raise RuntimeError("compilation of %s failed" % s)
     if jobs or not os.path.exists(LIB):
-        cmd = [NVCC] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs + ["-ldl", "-lpthread"]
+        cmd = [NVCC] + ARCH + ["-shared", "-Xcompiler", "-fPIC", "-o", LIB] + objs + [
+            "-L/usr/local/cuda/lib64", "-lcublas", "-lcusolver", "-ldl", "-lpthread",
+            "-Xlinker", "-rpath", "-Xlinker", "/usr/local/cuda/lib64"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

@@ -6,18 +6,26 @@
 #include <memory>
 #include <string>
 
+#include "hfx_dscf.hpp"
 #include "hfx_engine.hpp"
 #include "hfx_scf.hpp"
 
 struct hfx_job {
     std::unique_ptr<hfx::Job> job;
     std::unique_ptr<hfx::ScfSetup> setup;   // S, H, X, E_nuc; made on first SCF
+    std::unique_ptr<hfx::DeviceScf> dscf_rhf, dscf_uhf;   // device SCF workspaces
+    ~hfx_job()
+    {
+        dscf_rhf.reset();
+        dscf_uhf.reset();
+        job.reset();
+    }
 };
 
 namespace hfx {
 // density-weighted screening threshold of the FP64 builds of density changes
 // in the mixed-precision SCF (Q_AB Q_CD max|dD| below this: quartet skipped)
-constexpr double kDeltaThr = 1e-10;
+constexpr double kDeltaThr = 1e-12;
 void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG);   // hfx_noalloc.cu
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -305,13 +313,10 @@ hfx_status hfx_rhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, con
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
-        double fock_ms = 0.0;
-        GBuilder g = [&](const double* P, double* G, int mode) {
-            job.fock_rhf_ex(P, G, mode == BUILD_DEFAULT && job.mixed(), mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
-            fock_ms += job.stats.ms;
-        };
-        ScfOutput out = rhf_diis(b, o, P0, g);
-        fill_result(out, res, fock_ms);
+        ScfSetup setup = scf_setup(b);
+        DeviceScf d(job, setup, 1);
+        ScfOutput out = d.run(b, setup, o, 0, 0, P0, nullptr, kDeltaThr);
+        fill_result(out, res, out.fock_ms);
         int K = out.K;
         if (density) std::memcpy(density, out.P.data(), sizeof(double) * K * K);
         if (coefficient && !out.C.empty()) std::memcpy(coefficient, out.C.data(), sizeof(double) * K * K);
@@ -331,14 +336,10 @@ hfx_status hfx_uhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, int
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
-        double fock_ms = 0.0;
-        JKBuilder jk = [&](const double* a, const double* bb, double* J, double* Ka, double* Kb, int mode) {
-            job.fock_uhf_ex(a, bb, J, Ka, Kb, mode == BUILD_DEFAULT && job.mixed(),
-                            mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
-            fock_ms += job.stats.ms;
-        };
-        ScfOutput out = uhf_diis(b, o, n_alpha, n_beta, Pa0, Pb0, jk);
-        fill_result(out, res, fock_ms);
+        ScfSetup setup = scf_setup(b);
+        DeviceScf d(job, setup, 2);
+        ScfOutput out = d.run(b, setup, o, n_alpha, n_beta, Pa0, Pb0, kDeltaThr);
+        fill_result(out, res, out.fock_ms);
         int K = out.K;
         if (Pa) std::memcpy(Pa, out.P.data(), sizeof(double) * K * K);
         if (Pb) std::memcpy(Pb, out.P2.data(), sizeof(double) * K * K);
@@ -365,13 +366,9 @@ hfx_status hfx_job_rhf(hfx_job* job, const hfx_scf_options* opt, const double* P
         if (opt) o = *opt;
         const ScfSetup& setup = job_setup(job);
         Job& j = *job->job;
-        double fock_ms = 0.0;
-        GBuilder g = [&](const double* P, double* G, int mode) {
-            j.fock_rhf_ex(P, G, mode == BUILD_DEFAULT && j.mixed(), mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
-            fock_ms += j.stats.ms;
-        };
-        ScfOutput out = rhf_diis(j.basis(), setup, o, P0, g);
-        fill_result(out, res, fock_ms);
+        if (!job->dscf_rhf) job->dscf_rhf = std::make_unique<DeviceScf>(j, setup, 1);
+        ScfOutput out = job->dscf_rhf->run(j.basis(), setup, o, 0, 0, P0, nullptr, kDeltaThr);
+        fill_result(out, res, out.fock_ms);
         int K = out.K;
         if (density) std::memcpy(density, out.P.data(), sizeof(double) * K * K);
         if (coefficient && !out.C.empty()) std::memcpy(coefficient, out.C.data(), sizeof(double) * K * K);
@@ -389,14 +386,9 @@ hfx_status hfx_job_uhf(hfx_job* job, const hfx_scf_options* opt, int n_alpha, in
         if (opt) o = *opt;
         const ScfSetup& setup = job_setup(job);
         Job& j = *job->job;
-        double fock_ms = 0.0;
-        JKBuilder jk = [&](const double* a, const double* b, double* J, double* Ka, double* Kb, int mode) {
-            j.fock_uhf_ex(a, b, J, Ka, Kb, mode == BUILD_DEFAULT && j.mixed(),
-                          mode == BUILD_FP64_DELTA ? kDeltaThr : 0.0);
-            fock_ms += j.stats.ms;
-        };
-        ScfOutput out = uhf_diis(j.basis(), setup, o, n_alpha, n_beta, Pa0, Pb0, jk);
-        fill_result(out, res, fock_ms);
+        if (!job->dscf_uhf) job->dscf_uhf = std::make_unique<DeviceScf>(j, setup, 2);
+        ScfOutput out = job->dscf_uhf->run(j.basis(), setup, o, n_alpha, n_beta, Pa0, Pb0, kDeltaThr);
+        fill_result(out, res, out.fock_ms);
         int K = out.K;
         if (Pa) std::memcpy(Pa, out.P.data(), sizeof(double) * K * K);
         if (Pb) std::memcpy(Pb, out.P2.data(), sizeof(double) * K * K);

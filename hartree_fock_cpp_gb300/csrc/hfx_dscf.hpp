@@ -1,0 +1,47 @@
+// hfx_dscf.hpp -- SCF iterations with the O(K^3) algebra on the device.
+#pragma once
+
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include "hfx_engine.hpp"
+#include "hfx_scf.hpp"
+
+namespace hfx {
+
+class DeviceScf {
+public:
+    // nspin = 1 (RHF) or 2 (UHF)
+    DeviceScf(Job& job, const ScfSetup& setup, int nspin);
+    ~DeviceScf();
+    DeviceScf(const DeviceScf&) = delete;
+    DeviceScf& operator=(const DeviceScf&) = delete;
+
+    // Runs the SCF (semantics of hfx_scf.cpp) from the given initial
+    // densities (null = zero); na/nb used for UHF.  delta_thr: density-weighted
+    // screening of the FP64 builds of density changes (mixed precision).
+    ScfOutput run(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt, int na, int nb, const double* P0a,
+                  const double* P0b, double delta_thr);
+
+private:
+    void gemm(bool ta, const double* A, bool tb, const double* B, double* C, double alpha = 1.0, int kdim = 0);
+    void dot(const double* a, const double* b, int n, int slot);
+    void fetch(double* host, int count);
+    void axpby(double a, const double* A, double b, const double* B, double* C);
+    void build(int mode, double dthr);
+    void error_and_energy();
+    void diagonalise(const double* const* Fs, const int* nocc, double occ_factor);
+
+    Job& job_;
+    int K_, nspin_;
+    cudaStream_t st_ = nullptr;
+    cublasHandle_t blas_ = nullptr;
+    cusolverDnHandle_t solver_ = nullptr;
+    DevBuf<double> H_, S_, X_, T1_, T2_, Fp_, W_, work_, scal_, G_, dG_, Kr_;
+    DevBuf<double> P_[2], Pn_[2], F_[2], E_[2], C_[2], Gr_[2], Pr_[2], dP_[2], e_[2], Kx_[2], dK_[2];
+    DevBuf<int> info_;
+    int lwork_ = 0;
+    double fock_ms_ = 0.0;
+};
+
+}  // namespace hfx

@@ -329,6 +329,33 @@ void Job::compute_schwarz()
 
 void Job::schwarz_host(std::vector<double>& Q) const { Q = qbf_; }
 
+// Calls f(X, Y) for every unique shell-pair pair X >= Y with
+// Q_X Q_Y >= thr (all pairs if thr < 0), visiting only the survivors: the
+// pairs are scanned in decreasing Q order and the scan for X stops at the
+// first Q_Y below thr / Q_X.
+template <typename F>
+void Job::for_each_surviving_quartet(double thr, F&& f) const
+{
+    const int np = (int)hpairs_.size();
+    if (thr < 0.0) {
+        for (int X = 0; X < np; ++X)
+            for (int Y = 0; Y <= X; ++Y) f(X, Y);
+        return;
+    }
+    std::vector<int> order(np);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return qsh_[a] > qsh_[b]; });
+    for (int X = 0; X < np; ++X) {
+        if (qsh_[X] <= 0.0) continue;
+        const double need = thr / qsh_[X];
+        for (int r = 0; r < np; ++r) {
+            const int Y = order[r];
+            if (qsh_[Y] < need) break;
+            if (Y <= X) f(X, Y);
+        }
+    }
+}
+
 void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops,
                       double* prims) const
 {
@@ -338,13 +365,11 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     std::vector<double> cost;
     tasks.clear();
     maxacc = maxw = maxr = 1;
-    for (int X = 0; X < np; ++X)
-        for (int Y = 0; Y <= X; ++Y) {
-            if (thr >= 0.0 && qsh_[X] * qsh_[Y] < thr) continue;
-            int bra = X, ket = Y;
-            if (key(Y) > key(X)) std::swap(bra, ket);
-            tasks.push_back({bra, ket, hpairs_[bra].npp << 16});
-        }
+    for_each_surviving_quartet(thr, [&](int X, int Y) {
+        int bra = X, ket = Y;
+        if (key(Y) > key(X)) std::swap(bra, ket);
+        tasks.push_back({bra, ket, hpairs_[bra].npp << 16});
+    });
     std::vector<double> c(tasks.size());
     double fsum = 0.0, psum = 0.0;
     for (size_t t = 0; t < tasks.size(); ++t) {
@@ -381,10 +406,8 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         std::vector<double> cost;
     };
     std::vector<Bucket> small(2 * 100), warp(2);
-    for (int X = 0; X < np; ++X)
-        for (int Y = 0; Y <= X; ++Y) {
+    for_each_surviving_quartet(thr, [&](int X, int Y) {
             const double bound = qsh_[X] * qsh_[Y];
-            if (thr >= 0.0 && bound < thr) continue;
             int bra = X, ket = Y;
             if (pcof(Y) > pcof(X)) std::swap(bra, ket);
             const bool f32 = mixed && bound < tau;
@@ -404,7 +427,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 bk.t.push_back({bra, ket, i0 | (i1 << 16)});
                 bk.cost.push_back((double)(i1 - i0) * k.npp * fpp);
             }
-        }
+    });
     std::vector<Task> all;
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();

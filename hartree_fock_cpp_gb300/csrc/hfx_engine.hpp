@@ -160,6 +160,8 @@ private:
     void run_tasks(int mode, int nk, const std::vector<Task>* host_tasks, const DevBuf<Task>& tasks, int ntasks,
                    int maxacc, int maxw, int maxr, LaunchArgs a);
     LaunchArgs base_args() const;
+    template <typename F>
+    void for_each_surviving_quartet(double thr, F&& f) const;
     void record_stats(int launches);
 
     Basis basis_;

@@ -6,8 +6,11 @@
 //   T : the reference's per-axis kinetic form (integrals.hpp:122-177)
 //       T^x_ij = b(2j+1) S_ij - 2 b^2 S_i,j+2 - j(j-1)/2 S_i,j-2
 //   V = -sum_C Z_C 2 pi / p sum_tuv E_t E_u E_v R_tuv(p, P - C)
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "hfx_internal.hpp"
 
@@ -30,6 +33,43 @@ double boys_host(int m, double T)
     double e = std::exp(-T);
     for (int k = 0; k < m; ++k) F = ((2.0 * k + 1.0) * F - e) / (2.0 * T);
     return F;
+}
+
+// F_0..F_L(T) for the host integrals: table of accurate values at T_k = k/16
+// (built once from boys_host), 7-term Taylor for F_L, downward recursion;
+// asymptotic form with upward recursion beyond T = 36.
+static void boys_fast(int L, double T, double* F)
+{
+    constexpr int NM = 26, NT = 36 * 16 + 1;
+    static const std::vector<double> tab = [] {
+        std::vector<double> t((size_t)NT * (NM + 1));
+        for (int k = 0; k < NT; ++k) {
+            for (int m = 0; m < NM; ++m) t[(size_t)k * (NM + 1) + m] = boys_host(m, k / 16.0);
+            t[(size_t)k * (NM + 1) + NM] = std::exp(-k / 16.0);
+        }
+        return t;
+    }();
+    if (T < 36.0 && L + 6 < NM) {
+        int k = (int)(T * 16.0 + 0.5);
+        double nd = k / 16.0 - T;
+        const double* f = tab.data() + (size_t)k * (NM + 1);
+        static const double inv_fact[7] = {1.0, 1.0, 0.5, 1.0 / 6, 1.0 / 24, 1.0 / 120, 1.0 / 720};
+        double r = 0.0;
+        for (int j = 6; j >= 0; --j) r = r * nd + f[L + j] * inv_fact[j];
+        F[L] = r;
+        double x = 1.0 / 5040.0;
+        for (int j = 6; j >= 0; --j) x = x * nd + inv_fact[j];
+        double e = f[NM] * x;
+        for (int m = L - 1; m >= 0; --m) F[m] = (2.0 * T * F[m + 1] + e) / (2.0 * m + 1.0);
+        return;
+    }
+    if (T >= 36.0) {
+        double e = std::exp(-T);
+        F[0] = 0.5 * std::sqrt(M_PI / T);
+        for (int m = 0; m < L; ++m) F[m + 1] = ((2.0 * m + 1.0) * F[m] - e) / (2.0 * T);
+        return;
+    }
+    for (int m = 0; m <= L; ++m) F[m] = boys_host(m, T);
 }
 
 // 1-D Hermite expansion coefficients E^{ij}_t for i <= imax, j <= jmax,
@@ -67,7 +107,7 @@ static void hermite_R(int L, double p, double X, double Y, double Z, std::vector
     std::vector<double> cur((size_t)n * n * n, 0.0), nxt((size_t)n * n * n, 0.0);
     double T = p * (X * X + Y * Y + Z * Z);
     std::vector<double> F(L + 1);
-    for (int m = 0; m <= L; ++m) F[m] = boys_host(m, T);
+    boys_fast(L, T, F.data());
     auto id = [n](int t, int u, int v) { return ((size_t)t * n + u) * n + v; };
     // level m = L holds only R^{(L)}_{000}
     double pw = std::pow(-2.0 * p, L);
@@ -105,9 +145,16 @@ void one_electron(const Basis& b, std::vector<double>& S, std::vector<double>& T
     T.assign((size_t)K * K, 0.0);
     V.assign((size_t)K * K, 0.0);
     int natom = (int)b.atom_Z.size();
+    const int ns = (int)b.shells.size();
+    std::vector<std::pair<int, int>> pairs;
+    for (int sa = 0; sa < ns; ++sa)
+        for (int sb = 0; sb <= sa; ++sb) pairs.push_back({sa, sb});
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
     std::vector<double> Ex, Ey, Ez, R;
-    for (size_t sa = 0; sa < b.shells.size(); ++sa)
-        for (size_t sb = 0; sb <= sa; ++sb) {
+    for (size_t pi = next++; pi < pairs.size(); pi = next++) {
+        {
+            const int sa = pairs[pi].first, sb = pairs[pi].second;
             const Shell& A = b.shells[sa];
             const Shell& B = b.shells[sb];
             int na = ncart(A.L), nb = ncart(B.L);
@@ -172,6 +219,14 @@ void one_electron(const Basis& b, std::vector<double>& S, std::vector<double>& T
                     V[(size_t)I * K + J] = V[(size_t)J * K + I] = v[ca * nb + cb];
                 }
         }
+    }
+    };
+    // each shell pair writes its own blocks of S, T, V
+    const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads && (size_t)t < pairs.size(); ++t) th.emplace_back(worker);
+    worker();
+    for (auto& x : th) x.join();
 }
 
 }  // namespace hfx

@@ -27,6 +27,7 @@ struct ScfOutput {
     int fock_builds = 0;
     int mixed_builds = 0, fp64_builds = 0, delta_builds = 0;
     double seconds = 0;
+    double fock_ms = 0;
     std::vector<double> P, P2, C, e, e2;
 };
 
