@@ -64,6 +64,30 @@ class ScfResult(ctypes.Structure):
                 ("delta_builds", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("max_active", ctypes.c_int), ("hbm_budget_gb", ctypes.c_double), ("device", ctypes.c_int),
+                ("precision", ctypes.c_int), ("fp32_threshold", ctypes.c_double), ("reserved", ctypes.c_int * 8)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("mol", Molecule), ("method", ctypes.c_int), ("n_alpha", ctypes.c_int), ("n_beta", ctypes.c_int),
+                ("scf", ScfOptions), ("precision", ctypes.c_int), ("fp32_threshold", ctypes.c_double),
+                ("timeout_s", ctypes.c_double), ("inject_fault", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_int), ("status", ctypes.c_int), ("E_tot", ctypes.c_double),
+                ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("K", ctypes.c_int),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_end", ctypes.c_double),
+                ("fock_ms", ctypes.c_double), ("fock_builds", ctypes.c_int), ("message", ctypes.c_char * 256)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_int), ("running", ctypes.c_int), ("done", ctypes.c_int), ("failed", ctypes.c_int),
+                ("max_concurrent", ctypes.c_int), ("budget_bytes", ctypes.c_double),
+                ("in_use_bytes", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
+
+
 G_BUILDER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double))
 JK_BUILDER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
@@ -103,6 +127,15 @@ SIGNATURES = {
     "hfx_one_electron": (I, [V, V, V, V, P(I)]),
     "hfx_last_error": (I, [ctypes.c_char_p, ctypes.c_size_t]),
     "hfx_measure_peaks": (I, [I, P(D), P(D)]),
+    "hfx_server_create": (I, [V, P(V)]),
+    "hfx_server_submit": (I, [V, V, P(ctypes.c_longlong)]),
+    "hfx_server_poll": (I, [V, ctypes.c_longlong, V]),
+    "hfx_server_wait": (I, [V, ctypes.c_longlong, D, V]),
+    "hfx_server_cancel": (I, [V, ctypes.c_longlong]),
+    "hfx_server_drain": (I, [V, D]),
+    "hfx_server_density": (I, [V, ctypes.c_longlong, V, V]),
+    "hfx_server_stats": (I, [V, V]),
+    "hfx_server_destroy": (I, [V]),
 }
 
 

@@ -237,7 +237,7 @@ void DeviceScf::diagonalise(const double* const* Fs, const int* nocc, double occ
 }
 
 ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt_in, int na, int nb,
-                         const double* P0a, const double* P0b, double delta_thr)
+                         const double* P0a, const double* P0b, double delta_thr, const ScfControl* ctl)
 {
     auto t0 = std::chrono::steady_clock::now();
     hfx_scf_options opt = opt_in;
@@ -310,6 +310,14 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
     std::vector<double> Pswap;
     for (int it = 0; it < opt.max_iterations; ++it) {
         ++n_it;
+        if (ctl) {
+            if (ctl->cancel && ctl->cancel->load()) throw Error(HFX_ERR_CANCELLED, "job cancelled");
+            if (ctl->deadline > 0.0 &&
+                std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count() >
+                    ctl->deadline)
+                throw Error(HFX_ERR_TIMEOUT, "job exceeded its time limit");
+            if (ctl->fault_at_iteration == n_it) throw Error(HFX_ERR_NUMERIC, "injected fault at an SCF iteration");
+        }
         do_build();
         error_and_energy();
         // history slot

@@ -4,10 +4,21 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <atomic>
+
 #include "hfx_engine.hpp"
 #include "hfx_scf.hpp"
 
 namespace hfx {
+
+// Host-side control of a running SCF, checked between iterations (never
+// inside a kernel): cancellation flag, absolute deadline (steady clock,
+// seconds; 0 = none), and a test hook that fails the SCF at a given iteration.
+struct ScfControl {
+    std::atomic<bool>* cancel = nullptr;
+    double deadline = 0.0;
+    int fault_at_iteration = 0;
+};
 
 class DeviceScf {
 public:
@@ -21,7 +32,7 @@ public:
     // densities (null = zero); na/nb used for UHF.  delta_thr: density-weighted
     // screening of the FP64 builds of density changes (mixed precision).
     ScfOutput run(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt, int na, int nb, const double* P0a,
-                  const double* P0b, double delta_thr);
+                  const double* P0b, double delta_thr, const ScfControl* ctl = nullptr);
 
 private:
     void gemm(bool ta, const double* A, bool tb, const double* B, double* C, double alpha = 1.0, int kdim = 0);

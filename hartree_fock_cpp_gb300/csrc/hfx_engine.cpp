@@ -19,9 +19,83 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 
 namespace hfx {
+
+namespace {
+constexpr size_t kPoolMaxBlock = size_t(256) << 20;
+struct Pool {
+    std::mutex mu;
+    std::map<std::pair<int, size_t>, std::vector<void*>> free_blocks;   // (device, bucket) -> blocks
+    size_t cached = 0;
+};
+Pool& pool()
+{
+    static Pool* p = new Pool();   // never destroyed: blocks live until the process exits
+    return *p;
+}
+size_t bucket_of(size_t bytes)
+{
+    size_t b = 256;
+    while (b < bytes) b <<= 1;
+    return b;
+}
+}  // namespace
+
+void* pool_alloc(size_t bytes)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    void* p = nullptr;
+    if (bytes > kPoolMaxBlock) {
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            throw Error(HFX_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+        }
+        return p;
+    }
+    const size_t b = bucket_of(bytes);
+    {
+        std::lock_guard<std::mutex> lk(pool().mu);
+        auto it = pool().free_blocks.find({dev, b});
+        if (it != pool().free_blocks.end() && !it->second.empty()) {
+            p = it->second.back();
+            it->second.pop_back();
+            pool().cached -= b;
+            return p;
+        }
+    }
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(HFX_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    return p;
+}
+
+void pool_free(void* p, size_t bytes)
+{
+    if (!p) return;
+    if (bytes > kPoolMaxBlock) {
+        cudaFree(p);
+        return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const size_t b = bucket_of(bytes);
+    std::lock_guard<std::mutex> lk(pool().mu);
+    pool().free_blocks[{dev, b}].push_back(p);
+    pool().cached += b;
+}
+
+size_t pool_cached_bytes()
+{
+    std::lock_guard<std::mutex> lk(pool().mu);
+    return pool().cached;
+}
 
 void cuda_check(cudaError_t e, const char* what)
 {

@@ -29,6 +29,16 @@ bool is_small_class(int pcb, int pck);
 
 void cuda_check(cudaError_t e, const char* what);
 
+// Caching device allocator: freed blocks (rounded up to a power of two, up to
+// 256 MB) are kept for reuse instead of being returned with cudaFree, whose
+// implicit device synchronisation would stall every other job in flight when
+// one job of the request server finishes.  Larger blocks are allocated and
+// freed directly.  Callers free a block only after the work using it has
+// completed (a job synchronises its streams before its buffers go).
+void* pool_alloc(size_t bytes);
+void pool_free(void* p, size_t bytes);
+size_t pool_cached_bytes();
+
 // Owning device buffer.
 template <typename T>
 struct DevBuf {
@@ -40,7 +50,7 @@ struct DevBuf {
     ~DevBuf() { reset(); }
     void reset()
     {
-        if (p) cudaFree(p);
+        if (p) pool_free(p, n * sizeof(T));
         p = nullptr;
         n = 0;
     }
@@ -49,12 +59,7 @@ struct DevBuf {
         if (count == n && p) return;
         reset();
         if (count == 0) return;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e != cudaSuccess) {
-            p = nullptr;
-            cudaGetLastError();
-            throw Error(HFX_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-        }
+        p = static_cast<T*>(pool_alloc(count * sizeof(T)));
         n = count;
     }
     void upload(const std::vector<T>& v, cudaStream_t st)

@@ -16,6 +16,9 @@
 // ERI tensor is never stored.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
+
 #include "hfx_device.cuh"
 
 namespace hfx {
@@ -315,12 +318,29 @@ size_t generic_smem_bytes(int maxacc, int maxw, int maxr)
     return 6240 + sizeof(double) * (size_t)(maxacc + maxw + 2 * maxr + 16);
 }
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum once
+// per process: launches from concurrent jobs then never race on the attribute.
+template <typename K>
+static cudaError_t allow_max_smem_generic(K kern)
+{
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count((const void*)kern)) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (err == cudaSuccess) done.insert((const void*)kern);
+    return err;
+}
+
 cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
                            cudaStream_t st)
 {
     size_t sm = generic_smem_bytes(maxacc, maxw, maxr);
     auto go = [&](auto kern) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t e = allow_max_smem_generic(kern);
         if (e != cudaSuccess) return e;
         kern<<<grid, 128, sm, st>>>(a, maxacc, maxw, maxr);
         return cudaGetLastError();

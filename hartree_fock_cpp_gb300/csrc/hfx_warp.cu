@@ -18,6 +18,9 @@
 // recursion over m of integrals.hpp:541-618, driven by a neighbour table.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <set>
+
 #include "hfx_device.cuh"
 
 namespace hfx {
@@ -366,12 +369,29 @@ int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_
     return nab * ncd + w_nh(L1) * ncd + r;
 }
 
+// Raise a kernel's dynamic shared-memory limit to the device maximum once
+// per process: launches from concurrent jobs then never race on the attribute.
+template <typename K>
+static cudaError_t allow_max_smem(K kern)
+{
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count((const void*)kern)) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (err == cudaSuccess) done.insert((const void*)kern);
+    return err;
+}
+
 template <typename T>
 cudaError_t launch_warp_t(const WarpArgs<T>& a, int nk, int grid, int warps_per_cta, cudaStream_t st)
 {
     size_t sm = 8064 + sizeof(T) * (size_t)a.slice * warps_per_cta;
     auto go = [&](auto kern) -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t e = allow_max_smem(kern);
         if (e != cudaSuccess) return e;
         kern<<<grid, 32 * warps_per_cta, sm, st>>>(a);
         return cudaGetLastError();

@@ -254,6 +254,65 @@ hfx_status hfx_debug_pair_data(const hfx_molecule *mol, int *npairs, int *nprimp
 /* One-electron matrices S, T, V of a molecule (integrals.hpp:10-536), host. */
 hfx_status hfx_one_electron(const hfx_molecule *mol, double *S, double *T, double *V, int *K);
 
+/* ---- request server (continuous batching on one GPU) ---------------------- */
+
+typedef struct hfx_server hfx_server;
+
+typedef struct {
+    int max_active;          /* concurrent jobs (worker slots); default 8 */
+    double hbm_budget_gb;    /* device memory the jobs may hold; default 80% of free memory */
+    int device;
+    int precision;           /* default precision of requests (HFX_PREC_*) */
+    double fp32_threshold;   /* default mixed-precision cut */
+    int reserved[8];
+} hfx_server_options;
+
+enum { HFX_JOB_QUEUED = 0, HFX_JOB_RUNNING = 1, HFX_JOB_DONE = 2, HFX_JOB_FAILED = 3 };
+/* host-side fault injection (tests): fail the job at this stage */
+enum { HFX_FAULT_NONE = 0, HFX_FAULT_SETUP = 1, HFX_FAULT_OOM = 2, HFX_FAULT_ALLOC = 3, HFX_FAULT_ITERATION = 4 };
+
+typedef struct {
+    hfx_molecule mol;        /* copied at submission */
+    int method;              /* 0 RHF, 1 UHF */
+    int n_alpha, n_beta;     /* UHF occupations */
+    hfx_scf_options scf;
+    int precision;           /* -1: server default */
+    double fp32_threshold;   /* 0: server default */
+    double timeout_s;        /* 0: none; measured from submission */
+    int inject_fault;        /* HFX_FAULT_* (tests) */
+    int reserved[7];
+} hfx_request;
+
+typedef struct {
+    int state;               /* HFX_JOB_* */
+    hfx_status status;       /* HFX_OK, HFX_ERR_NOT_CONVERGED or the failure */
+    double E_tot;
+    int iterations, converged, K;
+    double t_submit, t_admit, t_end;   /* steady-clock seconds */
+    double fock_ms;
+    int fock_builds;
+    char message[256];
+} hfx_job_info;
+
+typedef struct {
+    int queued, running, done, failed, max_concurrent;
+    double budget_bytes, in_use_bytes;
+    int reserved[6];
+} hfx_server_stats_t;
+
+hfx_status hfx_server_create(const hfx_server_options *opt, hfx_server **server);
+hfx_status hfx_server_submit(hfx_server *server, const hfx_request *req, long long *id);
+hfx_status hfx_server_poll(hfx_server *server, long long id, hfx_job_info *info);
+/* wait for one job (timeout_s <= 0: no limit); HFX_ERR_TIMEOUT if it is still running */
+hfx_status hfx_server_wait(hfx_server *server, long long id, double timeout_s, hfx_job_info *info);
+hfx_status hfx_server_cancel(hfx_server *server, long long id);
+/* wait until the queue is empty and no job runs */
+hfx_status hfx_server_drain(hfx_server *server, double timeout_s);
+/* converged densities of a finished job (K*K each; Pb for UHF) */
+hfx_status hfx_server_density(hfx_server *server, long long id, double *Pa, double *Pb);
+hfx_status hfx_server_stats(hfx_server *server, hfx_server_stats_t *stats);
+hfx_status hfx_server_destroy(hfx_server *server);
+
 /* Last error message of the calling thread (empty if none). */
 hfx_status hfx_last_error(char *buf, size_t n);
 

@@ -1,0 +1,77 @@
+"""The request server: concurrent jobs give the same results as the same jobs
+run alone (energies within 1 uHa, iteration counts within +-1), and host-side
+faults fail only their own job with a status code."""
+import pytest
+
+import hartree_fock_cpp_gb300 as H
+from hartree_fock_cpp_gb300 import workloads as W
+from hartree_fock_cpp_gb300.server import Server
+
+pytestmark = pytest.mark.gpu
+E_TOL = 1e-6
+
+OH = [("O", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.83))]
+MIX = [
+    dict(config=W.water(), basis_set="STO-3G", method="RHF"),
+    dict(config=W.water(), basis_set="cc-pVDZ", method="RHF"),
+    dict(config=W.benzene(), basis_set="cc-pVDZ", method="RHF"),
+    dict(config=OH, basis_set="6-31G*", method="UHF", spin=(5, 4)),
+    dict(config=W.n_decane(), basis_set="6-31G*", method="RHF"),
+    dict(config=W.nacl_scan(8)[3], basis_set="cc-pVTZ", method="RHF"),
+]
+
+
+def _alone(job):
+    if job["method"] == "UHF":
+        return H.uhf_diis(job["config"], job["basis_set"], spin_occ=job["spin"])
+    return H.rhf_diis(job["config"], job["basis_set"])
+
+
+def test_results_same_alone_and_in_the_mix():
+    alone = [_alone(j) for j in MIX]
+    with Server(max_active=6) as srv:
+        ids = [srv.submit(**j) for j in MIX]
+        srv.drain(600)
+        infos = [srv.poll(i) for i in ids]
+        st = srv.stats()
+    assert st["max_concurrent"] >= 2
+    for j, a, inf in zip(MIX, alone, infos):
+        assert inf["state"] == "done", inf
+        assert inf["converged"]
+        assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL, (j["basis_set"], inf["E_tot"], a["E_tot"])
+        assert abs(inf["iterations"] - a["iterations"]) <= 1
+
+
+def test_faults_fail_only_their_own_job():
+    with Server(max_active=4) as srv:
+        good = srv.submit(W.water(), "STO-3G")
+        bad_basis = srv.submit(W.water(), "no-such-basis")
+        bad_elem = srv.submit([("Xx", (0.0, 0.0, 0.0)), ("H", (0.0, 0.0, 1.4))], "STO-3G")
+        oom = srv.submit(W.water(), "STO-3G", inject_fault="oom")
+        alloc = srv.submit(W.water(), "STO-3G", inject_fault="alloc")
+        it = srv.submit(W.water(), "STO-3G", inject_fault="iteration")
+        slow = srv.submit(W.benzene(), "cc-pVDZ", timeout_s=1e-3)
+        srv.drain(300)
+        g = srv.poll(good)
+        assert g["state"] == "done" and g["converged"]
+        assert srv.poll(bad_basis)["status"] == 2          # HFX_ERR_BASIS
+        assert srv.poll(bad_elem)["status"] == 2
+        assert srv.poll(oom)["status"] == 4                # HFX_ERR_OOM
+        assert srv.poll(alloc)["status"] == 4
+        assert srv.poll(it)["status"] == 9                 # HFX_ERR_NUMERIC (injected)
+        assert srv.poll(slow)["status"] == 8               # HFX_ERR_TIMEOUT
+        # the server keeps serving after the failures
+        after = srv.submit(W.water(), "STO-3G")
+        assert srv.wait(after, 120)["converged"]
+        st = srv.stats()
+        assert st["failed"] == 6 and st["running"] == 0
+
+
+def test_cancel_queued_job():
+    with Server(max_active=1) as srv:
+        first = srv.submit(W.benzene(), "cc-pVDZ")
+        second = srv.submit(W.water(), "STO-3G")
+        srv.cancel(second)
+        srv.drain(300)
+        assert srv.poll(first)["converged"]
+        assert srv.poll(second)["status"] == 7             # HFX_ERR_CANCELLED
