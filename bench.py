@@ -295,6 +295,11 @@ def run_engine(args):
         fbm.close()
         fb64.close()
 
+    # ---- served request stream: continuous batching vs one-at-a-time FP64 ----
+    served = None
+    if args.serve_jobs > 0:
+        served = serve_section(H, W, args.serve_jobs, local)
+
     # ---- e2e: through hfx_rhf_diis with host buffers -------------------------
     e2e_lat = []
     r = None
@@ -338,6 +343,7 @@ def run_engine(args):
         "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},
         "mixed_precision": mixed,
+        "served_stream": served,
         "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP64 FMA-loop peak of this GPU (hfx_measure_peaks, same run)",
@@ -353,6 +359,66 @@ def run_engine(args):
         torch.distributed.barrier()
 
 
+def serve_section(H, W, n_jobs, device, rate_factor=2.0, tau=0.03, max_it=60, seed=20261203):
+    """First n_jobs requests of the seeded served stream (random C/N/O/S trees,
+    80% RHF / 20% UHF doublets, STO-3G / 6-31G* / cc-pVDZ).  Baseline: the
+    plain FP64 GPU path one job at a time.  Served: Poisson arrivals at
+    rate_factor x the baseline throughput into the request server (mixed
+    precision, continuous batching); solves/s and p50/p99 time from arrival to
+    converged energy.  SCFs are capped at max_it iterations (non-converged
+    jobs count as finished, not solved)."""
+    from hartree_fock_cpp_gb300.server import Server
+    jobs = W.served_stream(n_jobs, seed=seed)
+    Ks = [H.basis_construction(j["config"], j["basis"]).K for j in jobs]
+    seq_lat, seq_E, seq_ok = [], [], 0
+    t0 = time.perf_counter()
+    for j in jobs:
+        t = time.perf_counter()
+        kw = dict(max_it=max_it)
+        r = (H.uhf_diis(j["config"], j["basis"], spin_occ=j["spin"], **kw) if j["method"] == "UHF"
+             else H.rhf_diis(j["config"], j["basis"], **kw))
+        seq_lat.append(time.perf_counter() - t)
+        seq_E.append(r["E_tot"] if r["converged"] else None)
+        seq_ok += int(r["converged"])
+    T_seq = time.perf_counter() - t0
+    mu = n_jobs / T_seq
+    # arrival-to-finish latency of the one-at-a-time path under the same arrival process
+    rng = np.random.default_rng(seed)
+    lam = rate_factor * mu
+    arrivals = np.cumsum(rng.exponential(1.0 / lam, size=n_jobs))
+    arrivals -= arrivals[0]
+    free_at, seq_resp = 0.0, []
+    for a, d in zip(arrivals, seq_lat):
+        start = max(a, free_at)
+        free_at = start + d
+        seq_resp.append(free_at - a)
+    with Server(max_active=16, device=device, precision=H.HFX_PREC_MIXED, fp32_threshold=tau) as srv:
+        ids = []
+        t0 = time.perf_counter()
+        for a, j in zip(arrivals, jobs):
+            dt = a - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(j["config"], j["basis"], method=j["method"], spin=j.get("spin"), max_it=max_it))
+        srv.drain(3600)
+        T_srv = time.perf_counter() - t0
+        infos = [srv.poll(i) for i in ids]
+        st = srv.stats()
+    lat = [i["t_end"] - i["t_submit"] for i in infos]
+    ok = sum(1 for i in infos if i["converged"])
+    dE = [abs(i["E_tot"] - e) for i, e in zip(infos, seq_E) if e is not None and i["converged"]]
+    return {"sample": "first %d requests of the seeded stream (seed %d), K %d..%d, max %d SCF iterations"
+                      % (n_jobs, seed, min(Ks), max(Ks), max_it),
+            "arrivals": "Poisson at %.1fx the one-at-a-time FP64 throughput" % rate_factor,
+            "one_at_a_time_fp64": {"solves_per_s": seq_ok / T_seq, "jobs_per_s": mu,
+                                   "p50_s": float(np.percentile(seq_resp, 50)), "p99_s": float(np.percentile(seq_resp, 99)),
+                                   "converged": seq_ok},
+            "served_mixed": {"solves_per_s": ok / T_srv, "jobs_per_s": n_jobs / T_srv,
+                             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                             "converged": ok, "max_concurrent": st["max_concurrent"], "fp32_threshold": tau,
+                             "max_abs_dE_vs_fp64": float(max(dE)) if dE else None}}
+
+
 def run_fock_only(args):
     """Small fixed case for profilers: one job, a few device Fock builds."""
     import torch
@@ -360,7 +426,7 @@ def run_fock_only(args):
     from hartree_fock_cpp_gb300 import workloads as W
     cfg = getattr(W, args.molecule)()
     prec = H.HFX_PREC_MIXED if args.precision == "mixed" else H.HFX_PREC_FP64
-    fb = H.FockBuilder(config=cfg, basis_set=args.basis, precision=prec)
+    fb = H.FockBuilder(config=cfg, basis_set=args.basis, precision=prec, fp32_threshold=args.tau)
     K = fb.K
     rng = np.random.default_rng(0)
     P = rng.normal(size=(K, K)) * 0.1
@@ -382,12 +448,14 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision section")
+    ap.add_argument("--serve-jobs", type=int, default=12, help="served-stream sample size (0: skip)")
     ap.add_argument("--fock-only", action="store_true",
                     help="profiling case: job setup + --builds device Fock builds of --molecule/--basis")
     ap.add_argument("--molecule", default="benzene", choices=["water", "benzene", "n_decane"])
     ap.add_argument("--basis", default="cc-pVDZ")
     ap.add_argument("--builds", type=int, default=2)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--tau", type=float, default=0.03, help="fock-only: FP32 Schwarz cut (mixed)")
     args = ap.parse_args()
     if args.fock_only:
         run_fock_only(args)

@@ -541,9 +541,12 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         for (size_t i : idx) {
             const HostPair& b = hpairs_[bk.t[i].bra];
             const HostPair& k = hpairs_[bk.t[i].ket];
+            // tier by slice size (powers of two), so that tasks with small
+            // slices are not held to the occupancy of the largest one
             int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true);
-            int wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - 8064) / (sl * elem[f])));
-            tiers[-wpc].push_back(i);
+            int tier = 0;
+            while ((512 << tier) < sl) ++tier;
+            tiers[tier].push_back(i);
         }
         for (auto& kv : tiers) {
             LaunchGroup g{};
