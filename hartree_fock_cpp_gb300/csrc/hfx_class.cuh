@@ -72,7 +72,7 @@ __host__ __device__ constexpr int coef_off(int la, int lb, int ab)
     return o;
 }
 __host__ __device__ constexpr int n_coef(int la, int lb) { return coef_off(la, lb, c_nc(la) * c_nc(lb)); }
-__host__ __device__ constexpr int rec_stride(int la, int lb) { return (4 + n_coef(la, lb) + 1) & ~1; }
+__host__ __device__ constexpr int rec_stride(int la, int lb) { return (5 + n_coef(la, lb) + 1) & ~1; }
 
 
 // F_0..F_L: table + Taylor for F_L and exp(-T), downward recursion; beyond
@@ -191,17 +191,18 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     const int ij1 = tk.ij >> 16;
     for (int ij = tk.ij & 0xffff; ij < ij1; ++ij) {
         const T* rb = recb + ij * SB;
-        const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
-        const T* cb = rb + 4;
+        const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
+        const T* cb = rb + 5;
         for (int kl = 0; kl < ket.npp; ++kl) {
             const T* rk = reck + kl * SK;
-            const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
-            const T* ck = rk + 4;
+            const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3), rq = __ldg(rk + 4);
+            const T* ck = rk + 5;
             const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
-            const T pq = p + q;
-            const T rho = p * q / pq;
+            // 1/sqrt(p+q) is the only root; 1/p, 1/q come with the records
+            const T rs = rsqrt(p + q);
+            const T rho = p * q * (rs * rs);
             const T Tv = rho * (X * X + Y * Y + Z * Z);
-            const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
+            const T pref = (T)34.98683665524972 * rp * rq * rs;   // 2 pi^{5/2} / (p q sqrt(p+q))
             T F[L + 1];
             boys_all<T, L>(Tv, a.boys, F);
             T sd[L + 1];

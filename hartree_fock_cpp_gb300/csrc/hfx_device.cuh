@@ -59,7 +59,7 @@ __host__ __device__ inline int shell_pair_id(int a, int b)
 }
 
 // Primitive-pair record of the class kernels, for a pair of class (l0, l1):
-//   [p, Px, Py, Pz, c_0 ... c_{ncoef-1}] padded to an even length, where the
+//   [p, Px, Py, Pz, 1/p, c_0 ... c_{ncoef-1}] padded to an even length, where the
 // c_k are the structurally non-zero Hermite->Cartesian coefficients
 //   c = w_i(a) w_j(b) E^x_{ax bx, t} E^y_{ay by, u} E^z_{az bz, v}
 // (weights = contraction coefficient x cart_norm, exp(-mu AB^2) included),
@@ -71,7 +71,9 @@ struct PairClassTab {
     int ab_off;    // offset of this class's ab_start table
     int k_off;     // offset of this class's per-coefficient tables
 };
-constexpr int kNumPairClasses = 10;   // (00) (10) (11) (20) (21) (22) (30) (31) (32) (33)
+constexpr int kNumPairClasses = 10;
+// shared-memory header of the warp kernel (index tables), bytes
+constexpr int kWarpSmemHeader = 11776;   // (00) (10) (11) (20) (21) (22) (30) (31) (32) (33)
 
 __host__ __device__ constexpr int dncart(int l) { return (l + 1) * (l + 2) / 2; }
 __host__ __device__ constexpr int dnherm(int L) { return (L + 1) * (L + 2) * (L + 3) / 6; }

@@ -219,7 +219,7 @@ const ClassTables& class_tables()
                     }
                 t.ab_start.push_back(k);
                 pt.ncoef = k;
-                pt.stride = (4 + k + 1) & ~1;
+                pt.stride = (5 + k + 1) & ~1;
                 t.tab.push_back(pt);
             }
         return t;
@@ -271,6 +271,7 @@ PairData build_pair_data(const Basis& basis)
                     pd.rec[rb + 1] = (a * S0.x + be * S1.x) / p;
                     pd.rec[rb + 2] = (a * S0.y + be * S1.y) / p;
                     pd.rec[rb + 3] = (a * S0.z + be * S1.z) / p;
+                    pd.rec[rb + 4] = 1.0 / p;
                     int kc = 0;
                     for (int c0 = 0; c0 < n0; ++c0) {
                         int ax, ay, az;
@@ -287,7 +288,7 @@ PairData build_pair_data(const Basis& basis)
                                                    Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
                                                    Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
                                         row[herm_index(t, u, v)] = c;
-                                        pd.rec[rb + 4 + kc++] = c;
+                                        pd.rec[rb + 5 + kc++] = c;
                                     }
                         }
                     }
@@ -564,8 +565,8 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * k.npp;
             }
             g.slice = (slice + 1) & ~1;
-            g.warps_per_cta = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - 8064) / (g.slice * elem[f])));
-            size_t sm = 8064 + elem[f] * (size_t)g.slice * g.warps_per_cta;
+            g.warps_per_cta = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - kWarpSmemHeader) / (g.slice * elem[f])));
+            size_t sm = kWarpSmemHeader + elem[f] * (size_t)g.slice * g.warps_per_cta;
             int ctas_per_sm = (int)std::max<size_t>(1, (228 * 1024) / (sm + 1024));
             long long need = ((long long)g.n + g.warps_per_cta - 1) / g.warps_per_cta;
             g.grid = (int)std::min<long long>(need, (long long)nsm_ * ctas_per_sm);

@@ -78,9 +78,31 @@ __device__ __forceinline__ void boys_top(T Tv, int L, const T* __restrict__ tab,
     }
 }
 
-// Seeds s_m = pref (-2 rho)^m F_m(T), m = 0..L, written to S[m * sstride].
+// 1/(2m+1), m = 0..15, for the downward Boys recursion
+__constant__ double c_inv_odd64[16] = {1.0,       1.0 / 3,  1.0 / 5,  1.0 / 7,  1.0 / 9,  1.0 / 11,
+                                       1.0 / 13,  1.0 / 15, 1.0 / 17, 1.0 / 19, 1.0 / 21, 1.0 / 23,
+                                       1.0 / 25,  1.0 / 27, 1.0 / 29, 1.0 / 31};
+__constant__ float c_inv_odd32[16] = {1.0f,       1.0f / 3,  1.0f / 5,  1.0f / 7,  1.0f / 9,  1.0f / 11,
+                                      1.0f / 13,  1.0f / 15, 1.0f / 17, 1.0f / 19, 1.0f / 21, 1.0f / 23,
+                                      1.0f / 25,  1.0f / 27, 1.0f / 29, 1.0f / 31};
 template <typename T>
-__device__ __forceinline__ void boys_seeds(T Tv, T rho, T pref, int L, const T* __restrict__ tab, T* S, int sstride)
+__device__ __forceinline__ T inv_odd(int m);
+template <>
+__device__ __forceinline__ double inv_odd<double>(int m)
+{
+    return c_inv_odd64[m];
+}
+template <>
+__device__ __forceinline__ float inv_odd<float>(int m)
+{
+    return c_inv_odd32[m];
+}
+
+// Seeds s_m = pref (-2 rho)^m F_m(T), m = 0..L, written to S[m * sstride];
+// inv_rho = 1/rho avoids a division.
+template <typename T>
+__device__ __forceinline__ void boys_seeds(T Tv, T rho, T inv_rho, T pref, int L, const T* __restrict__ tab, T* S,
+                                           int sstride)
 {
     T FL, e;
     bool table;
@@ -93,9 +115,9 @@ __device__ __forceinline__ void boys_seeds(T Tv, T rho, T pref, int L, const T* 
         for (int m = 0; m < L; ++m) pw *= m2r;
         S[L * sstride] = pw * F;
         T t2 = Tv + Tv;
-        T rm2r = (T)1 / m2r;
+        T rm2r = (T)-0.5 * inv_rho;
         for (int m = L - 1; m >= 0; --m) {
-            F = w_fma(t2, F, e) * ((T)1 / (T)(2 * m + 1));
+            F = w_fma(t2, F, e) * inv_odd<T>(m);
             pw *= rm2r;
             S[m * sstride] = pw * F;
         }
@@ -105,8 +127,10 @@ __device__ __forceinline__ void boys_seeds(T Tv, T rho, T pref, int L, const T* 
         T inv2T = (T)0.5 * rs * rs;
         T pw = pref;
         S[0] = pw * F;
+        T odd = (T)1;
         for (int m = 0; m < L; ++m) {
-            F = ((T)(2 * m + 1) * F - e) * inv2T;
+            F = (odd * F - e) * inv2T;
+            odd += (T)2;
             pw *= m2r;
             S[(m + 1) * sstride] = pw * F;
         }
@@ -117,7 +141,7 @@ __device__ __forceinline__ void boys_seeds(T Tv, T rho, T pref, int L, const T* 
 // nb[e] = dir | i1 << 2 | i2 << 11 | c2 << 20  (dir 0/1/2 = x/y/z).
 template <typename T>
 __device__ __forceinline__ void recur_lane(T X, T Y, T Z, int L, const T* S, int sstride, T* R, int rs,
-                                           const int* nb)
+                                           const int* nb, const T* cf)
 {
     R[0] = S[L * sstride];
     for (int n = L - 1; n >= 0; --n) {
@@ -127,7 +151,7 @@ __device__ __forceinline__ void recur_lane(T X, T Y, T Z, int L, const T* S, int
             int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511, c2 = (w >> 20) & 15;
             T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
             T val = xd * R[i1 * rs];
-            if (c2) val = w_fma((T)c2, R[i2 * rs], val);
+            if (c2) val = w_fma(cf[e], R[i2 * rs], val);
             R[e * rs] = val;
         }
         R[0] = S[n * sstride];
@@ -147,7 +171,8 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
     short* idx3 = reinterpret_cast<short*>(smem);                 // 2197 shorts (4394 B)
     int* nbt = reinterpret_cast<int*>(smem + 4400);               // 455 ints (1820 B) -> 6220
     int* clin = reinterpret_cast<int*>(smem + 6240);              // 455 ints -> 8060
-    T* wbase = reinterpret_cast<T*>(smem + 8064);
+    T* cft = reinterpret_cast<T*>(smem + 8064);                   // 455 T (recursion coefficients) -> 11704
+    T* wbase = reinterpret_cast<T*>(smem + kWarpSmemHeader);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     T* sl = wbase + (size_t)warp * a.slice;
@@ -191,6 +216,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             w = dir | (i1 << 2) | (i2 << 11) | (c2 << 20);
         }
         nbt[e] = w;
+        cft[e] = (T)((w >> 20) & 15);
     }
     __syncthreads();
 
@@ -226,7 +252,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         const int ij_end = task.ij >> 16;
         for (int ij = task.ij & 0xffff; ij < ij_end; ++ij) {
             const T* rb = rec + bra.rec_off + (long long)ij * cb.stride;
-            const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3);
+            const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
             for (int e = lane; e < nw; e += 32) W[e] = (T)0;
             __syncwarp();
             if (lane_mode) {
@@ -234,14 +260,15 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                     const int nb = min(32, ket.npp - kl0);
                     if (lane < nb) {
                         const T* rk = rec + ket.rec_off + (long long)(kl0 + lane) * ck.stride;
-                        const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
+                        const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),
+                                rq = __ldg(rk + 4);
                         const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
-                        const T pq = p + q;
-                        const T rho = p * q / pq;
+                        const T rs = rsqrt(p + q);
+                        const T rho = p * q * (rs * rs);
                         const T Tv = rho * (X * X + Y * Y + Z * Z);
-                        const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
-                        boys_seeds<T>(Tv, rho, pref, L, a.boys, Sd + lane, 32);
-                        recur_lane<T>(X, Y, Z, L, Sd + lane, 32, Ra + lane, 32, nbt);
+                        const T pref = (T)34.98683665524972 * rp * rq * rs;
+                        boys_seeds<T>(Tv, rho, (p + q) * rp * rq, pref, L, a.boys, Sd + lane, 32);
+                        recur_lane<T>(X, Y, Z, L, Sd + lane, 32, Ra + lane, 32, nbt, cft);
                     }
                     __syncwarp();
                     // stage 2: W[tuv][cd] += sum_b sum_k (+-) c_k R_b[tuv + tnp_k]
@@ -251,7 +278,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                         const int k0 = __ldg(abs_k + cd), k1 = __ldg(abs_k + cd + 1);
                         T s = (T)0;
                         for (int b = 0; b < nb; ++b) {
-                            const T* ck_ = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride + 4;
+                            const T* ck_ = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride + 5;
                             for (int k = k0; k < k1; ++k) {
                                 const int w = __ldg(kl_k + k);
                                 const T r = Ra[idx3[lt + (w & 16383)] * 32 + b];
@@ -266,14 +293,15 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             } else {
                 for (int kl = 0; kl < ket.npp; ++kl) {
                     const T* rk = rec + ket.rec_off + (long long)kl * ck.stride;
-                    const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3);
+                    const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),
+                            rq = __ldg(rk + 4);
                     const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
-                    const T pq = p + q;
-                    const T rho = p * q / pq;
+                    const T rs = rsqrt(p + q);
+                    const T rho = p * q * (rs * rs);
                     const T Tv = rho * (X * X + Y * Y + Z * Z);
-                    const T pref = (T)34.98683665524972 * rsqrt(pq) / (p * q);
+                    const T pref = (T)34.98683665524972 * rp * rq * rs;
                     // seeds: lane 0 (downward recursion is sequential in m)
-                    if (lane == 0) boys_seeds<T>(Tv, rho, pref, L, a.boys, Sd, 1);
+                    if (lane == 0) boys_seeds<T>(Tv, rho, (p + q) * rp * rq, pref, L, a.boys, Sd, 1);
                     __syncwarp();
                     // level-parallel recursion, ping-pong between Ra and Rb
                     T* prev = Ra;
@@ -291,7 +319,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                                 const int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511, c2 = (w >> 20) & 15;
                                 const T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
                                 val = xd * prev[i1];
-                                if (c2) val = w_fma((T)c2, prev[i2], val);
+                                if (c2) val = w_fma(cft[e], prev[i2], val);
                             }
                             cur[e] = val;
                         }
@@ -300,7 +328,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                         prev = cur;
                         cur = tmp;
                     }
-                    const T* ck_ = rk + 4;
+                    const T* ck_ = rk + 5;
                     for (int e = lane; e < nw; e += 32) {
                         const int tuv = e / ncd, cd = e - tuv * ncd;
                         const int lt = clin[tuv];
@@ -318,7 +346,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 }
             }
             // stage 3: bra transform, once per bra primitive pair
-            const T* cbp = rb + 4;
+            const T* cbp = rb + 5;
             for (int e = lane; e < nout; e += 32) {
                 const int ab = e / ncd, cd = e - ab * ncd;
                 const int k0 = __ldg(abs_b + ab), k1 = __ldg(abs_b + ab + 1);
@@ -392,7 +420,7 @@ static cudaError_t allow_max_smem(K kern)
 template <typename T>
 cudaError_t launch_warp_t(const WarpArgs<T>& a, int nk, int grid, int warps_per_cta, cudaStream_t st)
 {
-    size_t sm = 8064 + sizeof(T) * (size_t)a.slice * warps_per_cta;
+    size_t sm = kWarpSmemHeader + sizeof(T) * (size_t)a.slice * warps_per_cta;
     auto go = [&](auto kern) -> cudaError_t {
         cudaError_t e = allow_max_smem(kern);
         if (e != cudaSuccess) return e;
