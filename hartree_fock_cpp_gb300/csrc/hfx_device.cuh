@@ -177,6 +177,8 @@ struct WarpArgs {
     int lane_r;                // 1: lane-parallel R allowed for this launch
     const double* Dsh;         // per shell pair max |D| (density screening), or null
     double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
+    double* Qout_bf;           // Schwarz pass (NK = 0): BF-pair bounds out
+    unsigned long long* Qout_sh;   // Schwarz pass: per shell pair max bound (double bits)
 };
 
 #ifdef __CUDACC__

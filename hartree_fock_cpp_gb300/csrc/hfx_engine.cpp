@@ -364,29 +364,58 @@ void Job::run_tasks(int mode, int nk, const std::vector<Task>*, const DevBuf<Tas
 
 void Job::compute_schwarz()
 {
-    int np = (int)hpairs_.size();
-    std::vector<Task> t(np);
-    int maxacc = 0, maxw = 0, maxr = 0;
-    for (int p = 0; p < np; ++p) {
-        t[p] = {p, p, hpairs_[p].npp << 16};
-        int L = hpairs_[p].l0 + hpairs_[p].l1;
-        int nab = ncart(hpairs_[p].l0) * ncart(hpairs_[p].l1);
-        maxacc = std::max(maxacc, nab * nab);
-        maxw = std::max(maxw, nherm(L) * nab);
-        maxr = std::max(maxr, nherm(2 * L));
-    }
-    DevBuf<Task> dt;
-    dt.upload(t, stream_);
+    // Diagonal shell quartets (AB|AB) on the warp kernel (NK = 0 writes the
+    // BF-pair bounds sqrt((ab|ab)) and the per-pair maximum), tiered by the
+    // shared-memory slice each class needs.
+    const int np = (int)hpairs_.size();
     size_t npair_bf = (size_t)basis_.K * (basis_.K + 1) / 2;
     d_qbf_.alloc(npair_bf);
     d_qsh_.alloc(np);
     cuda_check(cudaMemsetAsync(d_qbf_.p, 0, npair_bf * sizeof(double), stream_), "memset");
     cuda_check(cudaMemsetAsync(d_qsh_.p, 0, np * sizeof(unsigned long long), stream_), "memset");
-    LaunchArgs a = base_args();
-    a.thr = -1.0;
-    a.Qout_bf = d_qbf_.p;
-    a.Qout_sh = d_qsh_.p;
-    run_tasks(MODE_SCHWARZ, 1, &t, dt, np, maxacc, maxw, maxr, a);
+    std::map<int, std::vector<Task>> tiers;
+    std::map<int, int> tier_slice;
+    for (int p = 0; p < np; ++p) {
+        const HostPair& h = hpairs_[p];
+        int sl = warp_slice_elems(h.l0, h.l1, h.l0, h.l1, h.npp, true);
+        int tier = 0;
+        while ((512 << tier) < sl) ++tier;
+        tiers[tier].push_back({p, p, h.npp << 16});
+        tier_slice[tier] = std::max(tier_slice[tier], sl);
+    }
+    std::vector<DevBuf<Task>> dts(tiers.size());
+    DevBuf<int> ctr;
+    ctr.alloc(tiers.size());
+    cuda_check(cudaMemsetAsync(ctr.p, 0, sizeof(int) * tiers.size(), stream_), "memset");
+    size_t ti = 0;
+    for (auto& kv : tiers) {
+        dts[ti].upload(kv.second, stream_);
+        const int slice = (tier_slice[kv.first] + 1) & ~1;
+        const int wpc = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - kWarpSmemHeader) / (slice * sizeof(double))));
+        const size_t sm = kWarpSmemHeader + sizeof(double) * (size_t)slice * wpc;
+        const int ctas_per_sm = (int)std::max<size_t>(1, (228 * 1024) / (sm + 1024));
+        const long long need = ((long long)kv.second.size() + wpc - 1) / wpc;
+        const int grid = (int)std::min<long long>(need, (long long)nsm_ * ctas_per_sm);
+        WarpArgs<double> a{};
+        a.pairs = d_pairs_.p;
+        a.rec = d_rec64_.p;
+        a.pct = d_pct_.p;
+        a.ab_start = d_abs_.p;
+        a.k_herm = d_kh_.p;
+        a.k_lin = d_kl_.p;
+        a.tasks = dts[ti].p;
+        a.ntasks = (int)kv.second.size();
+        a.counter = ctr.p + ti;
+        a.boys = d_boys_.p;
+        a.thr = -1.0;
+        a.K = basis_.K;
+        a.slice = slice;
+        a.lane_r = 1;
+        a.Qout_bf = d_qbf_.p;
+        a.Qout_sh = d_qsh_.p;
+        cuda_check(launch_warp(false, &a, 0, grid, wpc, stream_), "schwarz launch");
+        ++ti;
+    }
     qbf_.resize(npair_bf);
     std::vector<unsigned long long> qs(np);
     cuda_check(cudaMemcpyAsync(qbf_.data(), d_qbf_.p, npair_bf * sizeof(double), cudaMemcpyDeviceToHost, stream_),

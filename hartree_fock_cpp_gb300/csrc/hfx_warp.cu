@@ -357,6 +357,22 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             __syncwarp();
         }
 
+        // Schwarz pass: diagonal (ab|ab) of the diagonal shell quartet (AB|AB)
+        if constexpr (NK == 0) {
+            for (int e = lane; e < nout; e += 32) {
+                const int ab = e / ncd, cd = e - ab * ncd;
+                if (ab != cd) continue;
+                const int ia = ab / n1, ib = ab - ia * n1;
+                if (bra.same && ia < ib) continue;
+                const double v = (double)acc[e];
+                const double qv = sqrt(v > 0.0 ? v : 0.0);
+                a.Qout_bf[wpidx(bra.bf0 + ia, bra.bf1 + ib)] = qv;
+                atomicMax(a.Qout_sh + task.bra, (unsigned long long)__double_as_longlong(qv));
+            }
+            __syncwarp();
+            continue;
+        }
+
         // digestion (FP64)
         const int K = a.K;
         for (int e = lane; e < nout; e += 32) {
@@ -428,6 +444,7 @@ cudaError_t launch_warp_t(const WarpArgs<T>& a, int nk, int grid, int warps_per_
         return cudaGetLastError();
     };
     if (nk == 2) return go(k_warp_quartet<T, 2>);
+    if (nk == 0) return go(k_warp_quartet<T, 0>);
     return go(k_warp_quartet<T, 1>);
 }
 
