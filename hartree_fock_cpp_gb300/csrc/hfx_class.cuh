@@ -299,17 +299,15 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     }
 }
 
+// One thread per task, 128 threads per CTA; the kernel takes SmallArgs<T> by value.
 template <typename T, int LA, int LB, int LC, int LD>
-cudaError_t launch_small(const SmallArgs<T>& a, int nk, cudaStream_t st)
+cudaError_t small_spec(int nk, int ntasks, KernelSpec* s)
 {
-    if (a.ntasks == 0) return cudaSuccess;
-    const int block = 128;
-    const int grid = (a.ntasks + block - 1) / block;
-    if (nk == 2)
-        k_small<T, LA, LB, LC, LD, 2><<<grid, block, 0, st>>>(a);
-    else
-        k_small<T, LA, LB, LC, LD, 1><<<grid, block, 0, st>>>(a);
-    return cudaGetLastError();
+    s->func = nk == 2 ? (const void*)k_small<T, LA, LB, LC, LD, 2> : (const void*)k_small<T, LA, LB, LC, LD, 1>;
+    s->block = dim3(128);
+    s->grid = dim3((unsigned)((ntasks + 127) / 128));
+    s->smem = 0;
+    return cudaSuccess;
 }
 
 }  // namespace hfx

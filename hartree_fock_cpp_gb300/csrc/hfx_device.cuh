@@ -19,6 +19,14 @@
 
 namespace hfx {
 
+// Launch configuration of one kernel: the stream path hands it to
+// cudaLaunchKernel, the graph path to cudaGraphAddKernelNode.
+struct KernelSpec {
+    const void* func = nullptr;
+    dim3 grid, block;
+    size_t smem = 0;
+};
+
 constexpr int kBoysM = 20;          // orders stored (12 + 7 Taylor terms + 1)
 constexpr int kBoysInvStep = 16;    // grid step 1/16
 constexpr int kBoysTMax = 36;       // table covers [0, 36]; upward recursion beyond

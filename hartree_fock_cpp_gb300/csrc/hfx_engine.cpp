@@ -17,7 +17,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <tuple>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -125,6 +127,7 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
     if (opt_.screening_threshold == 0.0) opt_.screening_threshold = 1e-8;
     if (opt_.fp32_threshold == 0.0) opt_.fp32_threshold = 1e-7;
     device_ = opt_.device;
+    no_graphs_ = std::getenv("HFX_NO_GRAPHS") != nullptr;
     int ndev = 0;
     cuda_check(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
     if (device_ < 0 || device_ >= ndev) throw Error(HFX_ERR_INVALID, "invalid CUDA device ordinal");
@@ -176,6 +179,7 @@ Job::~Job()
     if (ev1_) cudaEventDestroy(ev1_);
     if (evk0_) cudaEventDestroy(evk0_);
     if (evk1_) cudaEventDestroy(evk1_);
+    clear_graphs();
     for (auto e : aux_ev_) cudaEventDestroy(e);
     for (auto st : aux_) cudaStreamDestroy(st);
     if (fork_ev_) cudaEventDestroy(fork_ev_);
@@ -500,6 +504,7 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
 
 void Job::build_jk_groups(bool mixed, GroupSet& gs)
 {
+    clear_graphs();   // graphs hold the previous plan's task pointers
     const double thr = opt_.screening_threshold;
     const double tau = opt_.fp32_threshold;
     const int np = (int)hpairs_.size();
@@ -619,64 +624,158 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     gs.tasks.upload(all, stream_);
 }
 
-void Job::launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
+StreamSink::StreamSink(cudaStream_t main, const std::vector<cudaStream_t>& aux, cudaEvent_t fork_ev,
+                       const std::vector<cudaEvent_t>& aux_ev)
+    : main_(main), aux_(aux), fork_ev_(fork_ev), aux_ev_(aux_ev)
+{
+}
+
+void StreamSink::zero(int lane, void* p, size_t bytes)
+{
+    cuda_check(cudaMemsetAsync(p, 0, bytes, stream(lane)), "memset");
+}
+
+void StreamSink::kernel(int lane, const KernelSpec& s, void** params)
+{
+    if (s.grid.x == 0) return;
+    cuda_check(cudaLaunchKernel(s.func, s.grid, s.block, params, s.smem, stream(lane)), "kernel launch");
+}
+
+void StreamSink::fork()
+{
+    cuda_check(cudaEventRecord(fork_ev_, main_), "fork");
+    for (auto st : aux_) cuda_check(cudaStreamWaitEvent(st, fork_ev_, 0), "fork wait");
+}
+
+void StreamSink::join()
+{
+    for (size_t i = 0; i < aux_.size(); ++i) {
+        cuda_check(cudaEventRecord(aux_ev_[i], aux_[i]), "join");
+        cuda_check(cudaStreamWaitEvent(main_, aux_ev_[i], 0), "join wait");
+    }
+}
+
+GraphSink::GraphSink(int lanes) : deps_(lanes) { cuda_check(cudaGraphCreate(&graph_, 0), "graph create"); }
+
+GraphSink::~GraphSink()
+{
+    if (graph_) cudaGraphDestroy(graph_);
+}
+
+void GraphSink::zero(int lane, void* p, size_t bytes)
+{
+    cudaMemsetParams mp{};
+    mp.dst = p;
+    mp.value = 0;
+    mp.elementSize = bytes % 4 == 0 ? 4 : 1;
+    mp.width = bytes / mp.elementSize;
+    mp.height = 1;
+    mp.pitch = 0;
+    cudaGraphNode_t node;
+    std::vector<cudaGraphNode_t>& d = deps_[lane];
+    cuda_check(cudaGraphAddMemsetNode(&node, graph_, d.data(), d.size(), &mp), "graph memset node");
+    d.assign(1, node);
+}
+
+void GraphSink::kernel(int lane, const KernelSpec& s, void** params)
+{
+    if (s.grid.x == 0) return;
+    cudaKernelNodeParams kp{};
+    kp.func = const_cast<void*>(s.func);
+    kp.gridDim = s.grid;
+    kp.blockDim = s.block;
+    kp.sharedMemBytes = (unsigned)s.smem;
+    kp.kernelParams = params;
+    kp.extra = nullptr;
+    cudaGraphNode_t node;
+    std::vector<cudaGraphNode_t>& d = deps_[lane];
+    cuda_check(cudaGraphAddKernelNode(&node, graph_, d.data(), d.size(), &kp), "graph kernel node");
+    d.assign(1, node);
+}
+
+void GraphSink::fork()
+{
+    for (size_t i = 1; i < deps_.size(); ++i) deps_[i] = deps_[0];
+}
+
+void GraphSink::join()
+{
+    std::vector<cudaGraphNode_t> all;
+    for (const auto& d : deps_)
+        for (auto n : d)
+            if (std::find(all.begin(), all.end(), n) == all.end()) all.push_back(n);
+    for (auto& d : deps_) d = all;
+}
+
+cudaGraphExec_t GraphSink::instantiate()
+{
+    cudaGraphExec_t exec = nullptr;
+    cuda_check(cudaGraphInstantiate(&exec, graph_, 0), "graph instantiate");
+    return exec;
+}
+
+void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
                     double* Kx2, int* counters, bool mixed_plan, double dthr)
 {
     const GroupSet& gs = plan(mixed_plan);
     const std::vector<LaunchGroup>& groups = gs.groups;
     const Task* tasks = gs.tasks.p;
     const double* Dsh = nullptr;
-    if (dthr > 0.0) {
-        cuda_check(launch_density_blocks(d_pairs_.p, (int)dpairs_host_.size(), Dk, Dk2, basis_.K, d_dsh_.p, stream_),
-                   "density blocks");
+    int K = basis_.K;
+    if (dthr > 0.0 && !dpairs_host_.empty()) {
+        const DPair* pr = d_pairs_.p;
+        int np = (int)dpairs_host_.size();
+        double* out = d_dsh_.p;
+        void* prm[] = {&pr, &np, &Dk, &Dk2, &K, &out};
+        sk.kernel(0, density_blocks_spec(np), prm);
         Dsh = d_dsh_.p;
     }
     int* ctr = counters ? counters : d_counters_.p;
-    cuda_check(cudaMemsetAsync(ctr, 0, sizeof(int) * std::max<size_t>(1, groups.size()), stream_), "memset counters");
-    cuda_check(cudaEventRecord(fork_ev_, stream_), "fork");
-    for (auto st : aux_) cuda_check(cudaStreamWaitEvent(st, fork_ev_, 0), "fork wait");
-    // warp groups (the long ones) on the main stream, small classes spread over the others
+    sk.zero(0, ctr, sizeof(int) * std::max<size_t>(1, groups.size()));
+    sk.fork();
+    // warp groups (the long ones) on the main lane, small classes spread over the others
+    const int naux = (int)aux_.size();
     int next_aux = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         const LaunchGroup& g = groups[gi];
         if (g.n == 0) continue;
-        cudaStream_t st = stream_;
+        KernelSpec ks;
         if (g.kind == 0) {
-            st = aux_[next_aux];
-            next_aux = (next_aux + 1) % (int)aux_.size();
-        }
-        cudaError_t e;
-        if (g.kind == 0) {
+            const int lane = 1 + next_aux;
+            next_aux = (next_aux + 1) % naux;
             if (g.fp32) {
                 SmallArgs<float> a{d_pairs_.p, d_rec32_.p, tasks + g.off, (int)g.n, d_boys32_.p,
-                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
-                e = launch_small_f32(g.pcb, g.pck, &a, nk, st);
+                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
+                cuda_check(small_spec_f32(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
+                void* prm[] = {&a};
+                sk.kernel(lane, ks, prm);
             } else {
                 SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys_.p,
-                                    opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
-                e = launch_small_f64(g.pcb, g.pck, &a, nk, st);
+                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
+                cuda_check(small_spec_f64(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
+                void* prm[] = {&a};
+                sk.kernel(lane, ks, prm);
             }
         } else {
+            cuda_check(warp_spec(g.fp32, nk, g.grid, g.warps_per_cta, g.slice, &ks), "warp kernel");
             if (g.fp32) {
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                   tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
-                                  opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                  opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
                                   Dsh, dthr};
-                e = launch_warp(true, &a, nk, g.grid, g.warps_per_cta, st);
+                void* prm[] = {&a};
+                sk.kernel(0, ks, prm);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                    tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
-                                   opt_.screening_threshold, d_qbf_.p, basis_.K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
                                    Dsh, dthr};
-                e = launch_warp(false, &a, nk, g.grid, g.warps_per_cta, st);
+                void* prm[] = {&a};
+                sk.kernel(0, ks, prm);
             }
         }
-        cuda_check(e, "class kernel launch");
     }
-    for (size_t s2 = 0; s2 < aux_.size(); ++s2) {
-        cuda_check(cudaEventRecord(aux_ev_[s2], aux_[s2]), "join");
-        cuda_check(cudaStreamWaitEvent(stream_, aux_ev_[s2], 0), "join wait");
-    }
+    sk.join();
 }
 
 void Job::record_stats(int launches) { record_stats_plan(launches, plan(mixed())); }
@@ -698,20 +797,95 @@ void Job::record_stats_plan(int launches, const GroupSet& gs)
 
 void Job::fock_rhf_device(const double* dP, double* dG) { fock_rhf_device_ex(dP, dG, mixed(), 0.0); }
 
+// Fock builds run as CUDA graphs after the first eager build of a variant
+// (RHF/UHF x plan x screening): the graph replays the accumulator clears, the
+// work-queue resets, every class launch on its stream and the symmetrisation,
+// reading the density from the job's input buffers and writing its output
+// buffers, so a build costs one graph launch plus two device copies.
+cudaGraphExec_t Job::graph_for(int nk, bool mixed_plan, double dthr)
+{
+    if (no_graphs_) return nullptr;
+    GraphEntry& g = graphs_[std::make_tuple(nk, mixed_plan, dthr)];
+    if (g.exec) return g.exec;
+    if (g.eager_runs < 1) return nullptr;   // the first build of a variant runs eagerly
+    const size_t n = (size_t)basis_.K * basis_.K;
+    d_gin_.alloc(n);
+    d_gout_.alloc(n);
+    if (nk == 2) {
+        d_gin2_.alloc(n);
+        d_gout2_.alloc(n);
+        d_gout3_.alloc(n);
+    }
+    GraphSink gsink(1 + (int)aux_.size());
+    if (nk == 1)
+        enqueue_rhf(gsink, d_gin_.p, d_gout_.p, mixed_plan, dthr);
+    else
+        enqueue_uhf(gsink, d_gin_.p, d_gin2_.p, d_gout_.p, d_gout2_.p, d_gout3_.p, mixed_plan, dthr);
+    g.exec = gsink.instantiate();
+    return g.exec;
+}
+
+void Job::clear_graphs()
+{
+    for (auto& kv : graphs_)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    graphs_.clear();
+}
+
+void Job::enqueue_rhf(OpSink& sk, const double* dP, double* dG, bool mixed_plan, double dthr)
+{
+    int K = basis_.K;
+    const size_t n = (size_t)K * K;
+    sk.zero(0, d_J_.p, n * sizeof(double));
+    sk.zero(0, d_K_.p, n * sizeof(double));
+    launch_jk(sk, 1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr, nullptr, mixed_plan, dthr);
+    const double* jp = d_J_.p;
+    const double* kp = d_K_.p;
+    void* prm[] = {&jp, &kp, &dG, &K};
+    sk.kernel(0, finish_rhf_spec(K), prm);
+}
+
+void Job::enqueue_uhf(OpSink& sk, const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb,
+                      bool mixed_plan, double dthr)
+{
+    int K = basis_.K;
+    int n = K * K;
+    sk.zero(0, d_J_.p, (size_t)n * sizeof(double));
+    sk.zero(0, d_K_.p, (size_t)n * sizeof(double));
+    sk.zero(0, d_K2_.p, (size_t)n * sizeof(double));
+    double* dj = d_Dj_.p;
+    void* pa[] = {&dPa, &dPb, &dj, &n};
+    sk.kernel(0, add_spec(n), pa);
+    launch_jk(sk, 2, d_Dj_.p, dPa, dPb, d_J_.p, d_K_.p, d_K2_.p, nullptr, mixed_plan, dthr);
+    const double* jp = d_J_.p;
+    const double* kp = d_K_.p;
+    const double* k2 = d_K2_.p;
+    void* prm[] = {&jp, &kp, &k2, &dJ, &dKa, &dKb, &K};
+    sk.kernel(0, finish_uhf_spec(K), prm);
+}
+
 void Job::fock_rhf_device_ex(const double* dP, double* dG, bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    int K = basis_.K;
-    size_t n = (size_t)K * K;
+    const int K = basis_.K;
+    const size_t n = (size_t)K * K;
     d_J_.alloc(n);
     d_K_.alloc(n);
+    cudaGraphExec_t ge = graph_for(1, mixed_plan, dthr);
     cuda_check(cudaEventRecord(ev0_, stream_), "event");
-    cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr, nullptr, mixed_plan, dthr);
-    cuda_check(cudaEventRecord(evk1_, stream_), "event");
-    cuda_check(launch_finish_rhf(d_J_.p, d_K_.p, dG, K, stream_), "finish");
+    if (ge) {
+        cuda_check(cudaMemcpyAsync(d_gin_.p, dP, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy in");
+        cuda_check(cudaEventRecord(evk0_, stream_), "event");
+        cuda_check(cudaGraphLaunch(ge, stream_), "graph launch");
+        cuda_check(cudaEventRecord(evk1_, stream_), "event");
+        cuda_check(cudaMemcpyAsync(dG, d_gout_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, stream_), "copy out");
+    } else {
+        cuda_check(cudaEventRecord(evk0_, stream_), "event");
+        StreamSink sk = stream_sink();
+        enqueue_rhf(sk, dP, dG, mixed_plan, dthr);
+        cuda_check(cudaEventRecord(evk1_, stream_), "event");
+        ++graphs_[std::make_tuple(1, mixed_plan, dthr)].eager_runs;
+    }
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats_plan((int)plan(mixed_plan).groups.size() + 1, plan(mixed_plan));
@@ -722,13 +896,17 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
     int K = basis_.K;
     size_t n = (size_t)K * K;
+    StreamSink sk = stream_sink();
     cuda_check(cudaEventRecord(ev0_, stream_), "event");
-    cuda_check(cudaMemsetAsync(Jacc, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaMemsetAsync(Kacc, 0, n * sizeof(double), stream_), "memset");
+    sk.zero(0, Jacc, n * sizeof(double));
+    sk.zero(0, Kacc, n * sizeof(double));
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters, mixed(), 0.0);
+    launch_jk(sk, 1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters, mixed(), 0.0);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
-    cuda_check(launch_finish_rhf(Jacc, Kacc, dG, K, stream_), "finish");
+    const double* jp = Jacc;
+    const double* kp = Kacc;
+    void* prm[] = {&jp, &kp, &dG, &K};
+    sk.kernel(0, finish_rhf_spec(K), prm);
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats((int)plan(mixed()).groups.size() + 1);
@@ -787,21 +965,31 @@ void Job::fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, d
                              bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    int K = basis_.K;
-    size_t n = (size_t)K * K;
+    const int K = basis_.K;
+    const size_t n = (size_t)K * K;
     d_J_.alloc(n);
     d_K_.alloc(n);
     d_K2_.alloc(n);
     d_Dj_.alloc(n);
+    cudaGraphExec_t ge = graph_for(2, mixed_plan, dthr);
     cuda_check(cudaEventRecord(ev0_, stream_), "event");
-    cuda_check(cudaMemsetAsync(d_J_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaMemsetAsync(d_K_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(cudaMemsetAsync(d_K2_.p, 0, n * sizeof(double), stream_), "memset");
-    cuda_check(launch_add(dPa, dPb, d_Dj_.p, (int)n, stream_), "add");
-    cuda_check(cudaEventRecord(evk0_, stream_), "event");
-    launch_jk(2, d_Dj_.p, dPa, dPb, d_J_.p, d_K_.p, d_K2_.p, nullptr, mixed_plan, dthr);
-    cuda_check(cudaEventRecord(evk1_, stream_), "event");
-    cuda_check(launch_finish_uhf(d_J_.p, d_K_.p, d_K2_.p, dJ, dKa, dKb, K, stream_), "finish");
+    if (ge) {
+        const size_t b = n * sizeof(double);
+        cuda_check(cudaMemcpyAsync(d_gin_.p, dPa, b, cudaMemcpyDeviceToDevice, stream_), "copy in");
+        cuda_check(cudaMemcpyAsync(d_gin2_.p, dPb, b, cudaMemcpyDeviceToDevice, stream_), "copy in");
+        cuda_check(cudaEventRecord(evk0_, stream_), "event");
+        cuda_check(cudaGraphLaunch(ge, stream_), "graph launch");
+        cuda_check(cudaEventRecord(evk1_, stream_), "event");
+        cuda_check(cudaMemcpyAsync(dJ, d_gout_.p, b, cudaMemcpyDeviceToDevice, stream_), "copy out");
+        cuda_check(cudaMemcpyAsync(dKa, d_gout2_.p, b, cudaMemcpyDeviceToDevice, stream_), "copy out");
+        cuda_check(cudaMemcpyAsync(dKb, d_gout3_.p, b, cudaMemcpyDeviceToDevice, stream_), "copy out");
+    } else {
+        cuda_check(cudaEventRecord(evk0_, stream_), "event");
+        StreamSink sk = stream_sink();
+        enqueue_uhf(sk, dPa, dPb, dJ, dKa, dKb, mixed_plan, dthr);
+        cuda_check(cudaEventRecord(evk1_, stream_), "event");
+        ++graphs_[std::make_tuple(2, mixed_plan, dthr)].eager_runs;
+    }
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats_plan((int)plan(mixed_plan).groups.size() + 2, plan(mixed_plan));

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
+#include <tuple>
 #include <vector>
 
 #include "hfx_device.cuh"
@@ -15,16 +17,15 @@ namespace hfx {
 size_t generic_smem_bytes(int maxacc, int maxw, int maxr);
 cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
                            cudaStream_t st);
-cudaError_t launch_finish_rhf(const double* Jacc, const double* Kacc, double* G, int K, cudaStream_t st);
-cudaError_t launch_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
-                              double* Kbo, int K, cudaStream_t st);
-cudaError_t launch_add(const double* A, const double* B, double* C, int n, cudaStream_t st);
-cudaError_t launch_small_f64(int pcb, int pck, const void* args, int nk, cudaStream_t st);
-cudaError_t launch_small_f32(int pcb, int pck, const void* args, int nk, cudaStream_t st);
+KernelSpec finish_rhf_spec(int K);   // k_finish_rhf(Jacc, Kacc, G, K)
+KernelSpec finish_uhf_spec(int K);   // k_finish_uhf(Jacc, Ka, Kb, J, Kao, Kbo, K)
+KernelSpec add_spec(int n);          // k_add(A, B, C, n)
+KernelSpec density_blocks_spec(int npairs);   // k_density_blocks(pairs, npairs, D1, D2, K, Dsh)
+cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<double>)
+cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<float>)
+cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s);
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
 int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
-cudaError_t launch_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
-                                  double* Dsh, cudaStream_t st);
 bool is_small_class(int pcb, int pck);
 
 void cuda_check(cudaError_t e, const char* what);
@@ -116,6 +117,54 @@ struct GroupSet {
     double flops64 = 0.0, flops32 = 0.0, prims = 0.0, quartets32 = 0.0;
 };
 
+// Destination of a Fock build's device work.  Lane 0 is the job's main
+// stream, lanes 1..n its auxiliary streams; fork() makes every auxiliary lane
+// wait for what lane 0 has issued so far, join() makes lane 0 wait for all of
+// them.  StreamSink issues the work on the streams as it comes; GraphSink
+// records it as the nodes and edges of a CUDA graph, built node by node
+// rather than by stream capture, so other threads' CUDA calls (allocations,
+// module loads, library handles of concurrent jobs) cannot invalidate it.
+class OpSink {
+public:
+    virtual ~OpSink() = default;
+    virtual void zero(int lane, void* p, size_t bytes) = 0;
+    virtual void kernel(int lane, const KernelSpec& s, void** params) = 0;
+    virtual void fork() = 0;
+    virtual void join() = 0;
+};
+
+class StreamSink final : public OpSink {
+public:
+    StreamSink(cudaStream_t main, const std::vector<cudaStream_t>& aux, cudaEvent_t fork_ev,
+               const std::vector<cudaEvent_t>& aux_ev);
+    void zero(int lane, void* p, size_t bytes) override;
+    void kernel(int lane, const KernelSpec& s, void** params) override;
+    void fork() override;
+    void join() override;
+
+private:
+    cudaStream_t stream(int lane) const { return lane == 0 ? main_ : aux_[lane - 1]; }
+    cudaStream_t main_;
+    const std::vector<cudaStream_t>& aux_;
+    cudaEvent_t fork_ev_;
+    const std::vector<cudaEvent_t>& aux_ev_;
+};
+
+class GraphSink final : public OpSink {
+public:
+    explicit GraphSink(int lanes);
+    ~GraphSink() override;
+    void zero(int lane, void* p, size_t bytes) override;
+    void kernel(int lane, const KernelSpec& s, void** params) override;
+    void fork() override;
+    void join() override;
+    cudaGraphExec_t instantiate();
+
+private:
+    cudaGraph_t graph_ = nullptr;
+    std::vector<std::vector<cudaGraphNode_t>> deps_;   // per lane: the nodes its next node depends on
+};
+
 class Job {
 public:
     Job(Basis b, const hfx_options& opt);
@@ -177,10 +226,23 @@ private:
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr, evk0_ = nullptr, evk1_ = nullptr;
 
     void build_jk_groups(bool mixed, GroupSet& gs);
-    void launch_jk(int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
+    void launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, const double* Dk2, double* J, double* Kx,
                    double* Kx2, int* counters = nullptr, bool mixed_plan = false, double dthr = 0.0);
     const GroupSet& plan(bool mixed_plan) const { return mixed_plan && mixed() ? gs_mixed_ : gs_fp64_; }
     void record_stats_plan(int launches, const GroupSet& gs);
+    StreamSink stream_sink() { return StreamSink(stream_, aux_, fork_ev_, aux_ev_); }
+    void enqueue_rhf(OpSink& sk, const double* dP, double* dG, bool mixed_plan, double dthr);
+    void enqueue_uhf(OpSink& sk, const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb, bool mixed_plan,
+                     double dthr);
+    cudaGraphExec_t graph_for(int nk, bool mixed_plan, double dthr);
+    void clear_graphs();
+    struct GraphEntry {
+        cudaGraphExec_t exec = nullptr;
+        int eager_runs = 0;
+    };
+    std::map<std::tuple<int, bool, double>, GraphEntry> graphs_;
+    bool no_graphs_ = false;
+    DevBuf<double> d_gin_, d_gin2_, d_gout_, d_gout2_, d_gout3_;
 
     std::vector<HostPair> hpairs_;
     GroupSet gs_fp64_, gs_mixed_;

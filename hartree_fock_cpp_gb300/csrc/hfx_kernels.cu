@@ -16,6 +16,7 @@
 // ERI tensor is never stored.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <set>
 
@@ -304,12 +305,13 @@ __global__ void k_density_blocks(const DPair* pairs, int npairs, const double* D
     Dsh[p] = m;
 }
 
-cudaError_t launch_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
-                                  double* Dsh, cudaStream_t st)
+KernelSpec density_blocks_spec(int npairs)
 {
-    if (npairs == 0) return cudaSuccess;
-    k_density_blocks<<<(npairs + 127) / 128, 128, 0, st>>>(pairs, npairs, D1, D2, K, Dsh);
-    return cudaGetLastError();
+    KernelSpec s;
+    s.func = (const void*)k_density_blocks;
+    s.grid = dim3((unsigned)((npairs + 127) / 128));
+    s.block = dim3(128);
+    return s;
 }
 
 // Host-side launch helpers (called from hfx_engine.cpp).
@@ -354,31 +356,19 @@ cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, in
     return go(k_quartet_generic<MODE_JK, 1>);
 }
 
-cudaError_t launch_finish_rhf(const double* Jacc, const double* Kacc, double* G, int K, cudaStream_t st)
+// Grid-stride elementwise kernels: 256 threads, at most 1024 CTAs.
+static KernelSpec elementwise_spec(const void* func, long long n)
 {
-    int n = K * K;
-    int grid = (n + 255) / 256;
-    if (grid > 1024) grid = 1024;
-    k_finish_rhf<<<grid, 256, 0, st>>>(Jacc, Kacc, G, K);
-    return cudaGetLastError();
+    KernelSpec s;
+    s.func = func;
+    long long grid = (n + 255) / 256;
+    s.grid = dim3((unsigned)std::max(1LL, std::min(grid, 1024LL)));
+    s.block = dim3(256);
+    return s;
 }
 
-cudaError_t launch_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
-                              double* Kbo, int K, cudaStream_t st)
-{
-    int n = K * K;
-    int grid = (n + 255) / 256;
-    if (grid > 1024) grid = 1024;
-    k_finish_uhf<<<grid, 256, 0, st>>>(Jacc, Ka, Kb, J, Kao, Kbo, K);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_add(const double* A, const double* B, double* C, int n, cudaStream_t st)
-{
-    int grid = (n + 255) / 256;
-    if (grid > 1024) grid = 1024;
-    k_add<<<grid, 256, 0, st>>>(A, B, C, n);
-    return cudaGetLastError();
-}
+KernelSpec finish_rhf_spec(int K) { return elementwise_spec((const void*)k_finish_rhf, (long long)K * K); }
+KernelSpec finish_uhf_spec(int K) { return elementwise_spec((const void*)k_finish_uhf, (long long)K * K); }
+KernelSpec add_spec(int n) { return elementwise_spec((const void*)k_add, n); }
 
 }  // namespace hfx

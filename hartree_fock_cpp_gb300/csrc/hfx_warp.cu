@@ -434,24 +434,35 @@ static cudaError_t allow_max_smem(K kern)
 }
 
 template <typename T>
-cudaError_t launch_warp_t(const WarpArgs<T>& a, int nk, int grid, int warps_per_cta, cudaStream_t st)
+static cudaError_t warp_spec_t(int nk, int grid, int warps_per_cta, int slice, KernelSpec* s)
 {
-    size_t sm = kWarpSmemHeader + sizeof(T) * (size_t)a.slice * warps_per_cta;
-    auto go = [&](auto kern) -> cudaError_t {
-        cudaError_t e = allow_max_smem(kern);
-        if (e != cudaSuccess) return e;
-        kern<<<grid, 32 * warps_per_cta, sm, st>>>(a);
-        return cudaGetLastError();
+    auto pick = [&](auto kern) -> cudaError_t {
+        s->func = (const void*)kern;
+        return allow_max_smem(kern);
     };
-    if (nk == 2) return go(k_warp_quartet<T, 2>);
-    if (nk == 0) return go(k_warp_quartet<T, 0>);
-    return go(k_warp_quartet<T, 1>);
+    cudaError_t e = nk == 2 ? pick(k_warp_quartet<T, 2>) : nk == 0 ? pick(k_warp_quartet<T, 0>) : pick(k_warp_quartet<T, 1>);
+    s->grid = dim3((unsigned)grid);
+    s->block = dim3((unsigned)(32 * warps_per_cta));
+    s->smem = kWarpSmemHeader + sizeof(T) * (size_t)slice * warps_per_cta;
+    return e;
+}
+
+// Launch configuration of k_warp_quartet<T, nk> (T = float when fp32); also
+// raises the kernel's shared-memory limit the first time it is asked for.
+cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s)
+{
+    return fp32 ? warp_spec_t<float>(nk, grid, warps_per_cta, slice, s)
+                : warp_spec_t<double>(nk, grid, warps_per_cta, slice, s);
 }
 
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st)
 {
-    if (fp32) return launch_warp_t<float>(*(const WarpArgs<float>*)args, nk, grid, warps_per_cta, st);
-    return launch_warp_t<double>(*(const WarpArgs<double>*)args, nk, grid, warps_per_cta, st);
+    const int slice = fp32 ? ((const WarpArgs<float>*)args)->slice : ((const WarpArgs<double>*)args)->slice;
+    KernelSpec s;
+    cudaError_t e = warp_spec(fp32, nk, grid, warps_per_cta, slice, &s);
+    if (e != cudaSuccess) return e;
+    void* prm[] = {const_cast<void*>(args)};
+    return cudaLaunchKernel(s.func, s.grid, s.block, prm, s.smem, st);
 }
 
 }  // namespace hfx
