@@ -26,7 +26,7 @@ from ._lib import BASIS_PATH, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError, check, li
 
 __all__ = ["Basis", "basis_construction", "schwarz_bounds", "ERI_GPU", "FockBuilder", "rhf_diis", "uhf_diis",
            "one_electron", "measure_peaks", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED", "BASIS_PATH",
-           "eri_index", "pair_index"]
+           "eri_index", "pair_index", "batch_scf"]
 
 
 def pair_index(a, b):                     # indexing.hpp:33-40
@@ -267,6 +267,49 @@ def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_
                 fock_builds=r.fock_builds, mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds,
                 delta_builds=r.delta_builds, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
                 BasisSet=basis_set, charge=charge)
+
+
+def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsilon=1e-6, damping=0.3,
+              screening_threshold=1e-8, energy_threshold=0.0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
+              max_parallel=0, param_path=None):
+    """Lockstep batched SCF (hfx_batch_scf): `molecules` is a list of
+    (config, basis_set); all of them iterate together on one packed job, one
+    Fock build per SCF cycle over every molecule still iterating.  The
+    batched counterpart of the reference's sequential scan drivers
+    (run.hpp:300-423, 498-577); every molecule starts from the zero density.
+    UHF takes spins = [(n_alpha, n_beta), ...].  Returns (results, stats):
+    one dict per molecule (E_tot, iterations, converged, ...) and the batch's
+    timing."""
+    n = len(molecules)
+    if n == 0:
+        return [], {}
+    uhf = method.upper() == "UHF"
+    if uhf and (spins is None or len(spins) != n):
+        raise HfxError(1, "batch UHF needs one (n_alpha, n_beta) per molecule")
+    args = [_lib.MoleculeArgs(cfg, bs, param_path) for cfg, bs in molecules]
+    mols = (_lib.Molecule * n)(*[a.c for a in args])
+    na = nb = None
+    if uhf:
+        na = np.ascontiguousarray([int(s[0]) for s in spins], dtype=np.int32)
+        nb = np.ascontiguousarray([int(s[1]) for s in spins], dtype=np.int32)
+    o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
+                     fp32_threshold)
+    bo = _lib.BatchOptions()
+    bo.method = 1 if uhf else 0
+    bo.max_parallel = int(max_parallel)
+    res = (_lib.ScfResult * n)()
+    st = _lib.BatchStats()
+    status = lib.hfx_batch_scf(ctypes.cast(mols, ctypes.c_void_p), n, ptr(na), ptr(nb), ctypes.byref(o),
+                               ctypes.byref(bo), ctypes.cast(res, ctypes.c_void_p), ctypes.byref(st))
+    if status not in (0, 6):
+        check(status)
+    out = [dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
+                K=r.K, duration=r.seconds, fock_ms=r.fock_ms, fock_builds=r.fock_builds,
+                mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds, delta_builds=r.delta_builds)
+           for r in res]
+    stats = dict(seconds=st.seconds, setup_seconds=st.setup_seconds, cycles=st.cycles, molecules=st.molecules,
+                 build_ms=st.build_ms, quartets=st.quartets, flops_fp64=st.flops_fp64)
+    return out, stats
 
 
 def one_electron(config, basis_set, param_path=None):

@@ -88,6 +88,16 @@ class ServerStats(ctypes.Structure):
                 ("in_use_bytes", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("max_parallel", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("seconds", ctypes.c_double), ("setup_seconds", ctypes.c_double), ("cycles", ctypes.c_int),
+                ("molecules", ctypes.c_int), ("build_ms", ctypes.c_double), ("quartets", ctypes.c_double),
+                ("flops_fp64", ctypes.c_double), ("reserved", ctypes.c_double * 5)]
+
+
 G_BUILDER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double))
 JK_BUILDER = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
@@ -136,6 +146,7 @@ SIGNATURES = {
     "hfx_server_density": (I, [V, ctypes.c_longlong, V, V]),
     "hfx_server_stats": (I, [V, V]),
     "hfx_server_destroy": (I, [V]),
+    "hfx_batch_scf": (I, [V, I, V, V, V, V, V, V]),
 }
 
 

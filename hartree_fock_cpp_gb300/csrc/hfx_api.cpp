@@ -165,7 +165,8 @@ hfx_status hfx_debug_pair_data(const hfx_molecule* mol, int* npairs, int* nprimp
 {
     return guarded([&] {
         if (!mol) throw Error(HFX_ERR_INVALID, "null molecule");
-        PairData pd = build_pair_data(build_basis(*mol));
+        const Basis b = build_basis(*mol);
+        PairData pd = build_pair_data(b, single_fragment(b));
         if (npairs) *npairs = (int)pd.dpairs.size();
         if (nprimpairs) *nprimpairs = (int)pd.geo.size();
         if (nepool) *nepool = (long long)pd.epool.size();

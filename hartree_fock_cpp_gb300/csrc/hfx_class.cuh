@@ -178,6 +178,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     const Task tk = a.tasks[task];
     const DPair bra = a.pairs[tk.bra];
     const DPair ket = a.pairs[tk.ket];
+    if (molecule_inactive(bra, a.active)) return;
     if (density_negligible(bra, ket, a.Dsh, a.dthr)) return;
 
     T acc[NAB][NCD];
@@ -263,15 +264,22 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
         }
     }
 
-    // digestion (FP64)
-    const int K = a.K;
+    // digestion (FP64), into the bra pair's molecule's matrices
+    const int K = bra.kdim;
+    const double* __restrict__ Qbf = a.Qbf + bra.qoff;
+    const double* __restrict__ Dj = a.Dj + bra.moff;
+    const double* __restrict__ Dk = a.Dk + bra.moff;
+    const double* __restrict__ Dk2 = a.Dk2 + (NK == 2 ? bra.moff : 0);
+    double* J = a.J + bra.moff;
+    double* Kx = a.Kx + bra.moff;
+    double* Kx2 = a.Kx2 + (NK == 2 ? bra.moff : 0);
     const bool same_pair = (tk.bra == tk.ket);
 #pragma unroll
     for (int ab = 0; ab < NAB; ++ab) {
         const int ia = ab / NB, ib = ab % NB;
         const int i = bra.bf0 + ia, j = bra.bf1 + ib;
         const long long pij = spidx(i, j);
-        const double qb = __ldg(a.Qbf + pij);
+        const double qb = __ldg(Qbf + pij);
         if (bra.same && ia < ib) continue;
 #pragma unroll
         for (int cd = 0; cd < NCD; ++cd) {
@@ -280,20 +288,20 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             if (ket.same && ic < id) continue;
             const long long pkl = spidx(k, l);
             if (same_pair && pij < pkl) continue;
-            if (a.thr >= 0.0 && qb * __ldg(a.Qbf + pkl) < a.thr) continue;
+            if (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr) continue;
             const double v =
                 (double)acc[ab][cd] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
-            atomicAdd(a.J + (long long)i * K + j, __ldg(a.Dj + (long long)k * K + l) * v);
-            atomicAdd(a.J + (long long)k * K + l, __ldg(a.Dj + (long long)i * K + j) * v);
-            atomicAdd(a.Kx + (long long)i * K + k, __ldg(a.Dk + (long long)j * K + l) * v);
-            atomicAdd(a.Kx + (long long)j * K + l, __ldg(a.Dk + (long long)i * K + k) * v);
-            atomicAdd(a.Kx + (long long)i * K + l, __ldg(a.Dk + (long long)j * K + k) * v);
-            atomicAdd(a.Kx + (long long)j * K + k, __ldg(a.Dk + (long long)i * K + l) * v);
+            atomicAdd(J + (long long)i * K + j, __ldg(Dj + (long long)k * K + l) * v);
+            atomicAdd(J + (long long)k * K + l, __ldg(Dj + (long long)i * K + j) * v);
+            atomicAdd(Kx + (long long)i * K + k, __ldg(Dk + (long long)j * K + l) * v);
+            atomicAdd(Kx + (long long)j * K + l, __ldg(Dk + (long long)i * K + k) * v);
+            atomicAdd(Kx + (long long)i * K + l, __ldg(Dk + (long long)j * K + k) * v);
+            atomicAdd(Kx + (long long)j * K + k, __ldg(Dk + (long long)i * K + l) * v);
             if constexpr (NK == 2) {
-                atomicAdd(a.Kx2 + (long long)i * K + k, __ldg(a.Dk2 + (long long)j * K + l) * v);
-                atomicAdd(a.Kx2 + (long long)j * K + l, __ldg(a.Dk2 + (long long)i * K + k) * v);
-                atomicAdd(a.Kx2 + (long long)i * K + l, __ldg(a.Dk2 + (long long)j * K + k) * v);
-                atomicAdd(a.Kx2 + (long long)j * K + k, __ldg(a.Dk2 + (long long)i * K + l) * v);
+                atomicAdd(Kx2 + (long long)i * K + k, __ldg(Dk2 + (long long)j * K + l) * v);
+                atomicAdd(Kx2 + (long long)j * K + l, __ldg(Dk2 + (long long)i * K + k) * v);
+                atomicAdd(Kx2 + (long long)i * K + l, __ldg(Dk2 + (long long)j * K + k) * v);
+                atomicAdd(Kx2 + (long long)j * K + k, __ldg(Dk2 + (long long)i * K + l) * v);
             }
         }
     }

@@ -56,8 +56,17 @@ struct __align__(16) DPair {
     double qmax;       // max_ab sqrt((ab|ab)) over the pair's BF pairs
     long long rec_off; // offset of the first primitive-pair record (elements)
     int pc;            // pair class l0*(l0+1)/2 + l1
-    int sh0, sh1;      // shell indices of shell 0 / shell 1 (reference order)
-    int pad;
+    int sh0, sh1;      // shell indices of shell 0 / shell 1 within the pair's molecule
+    // A packed job holds several molecules: the pair's basis-function and
+    // shell indices are local to its molecule, whose K x K matrices start at
+    // element moff of the packed D/J/K buffers (row stride kdim) and whose
+    // BF-pair Schwarz table starts at qoff.  A single-molecule job has
+    // frag = 0, pbase = 0, moff = qoff = 0 and kdim = K.
+    int kdim;          // basis functions of the pair's molecule
+    int pbase;         // pair id of the molecule's first shell pair
+    int frag;          // molecule index
+    long long moff;    // first element of the molecule's matrices in the packed buffers
+    long long qoff;    // first element of the molecule's BF-pair Schwarz bounds
 };
 
 // Triangular index of a shell pair (the pair array's order).
@@ -157,6 +166,7 @@ struct SmallArgs {
     double* Kx2;
     const double* Dsh;         // per shell pair max |D| (density screening), or null
     double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
+    const unsigned char* active;   // packed jobs: per molecule, 0 = skip its quartets (null: all)
 };
 
 // Arguments of the warp-per-shell-quartet kernel.
@@ -187,6 +197,7 @@ struct WarpArgs {
     double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
     double* Qout_bf;           // Schwarz pass (NK = 0): BF-pair bounds out
     unsigned long long* Qout_sh;   // Schwarz pass: per shell pair max bound (double bits)
+    const unsigned char* active;   // packed jobs: per molecule, 0 = skip its quartets (null: all)
 };
 
 #ifdef __CUDACC__
@@ -195,12 +206,19 @@ struct WarpArgs {
 __device__ __forceinline__ bool density_negligible(const DPair& b, const DPair& k, const double* Dsh, double dthr)
 {
     if (dthr <= 0.0) return false;
+    const double* D = Dsh + b.pbase;
     double d = fmax(Dsh[b.id], Dsh[k.id]);
-    d = fmax(d, Dsh[shell_pair_id(b.sh0, k.sh0)]);
-    d = fmax(d, Dsh[shell_pair_id(b.sh0, k.sh1)]);
-    d = fmax(d, Dsh[shell_pair_id(b.sh1, k.sh0)]);
-    d = fmax(d, Dsh[shell_pair_id(b.sh1, k.sh1)]);
+    d = fmax(d, D[shell_pair_id(b.sh0, k.sh0)]);
+    d = fmax(d, D[shell_pair_id(b.sh0, k.sh1)]);
+    d = fmax(d, D[shell_pair_id(b.sh1, k.sh0)]);
+    d = fmax(d, D[shell_pair_id(b.sh1, k.sh1)]);
     return b.qmax * k.qmax * d < dthr;
+}
+
+// Quartet of a molecule that takes no part in this build of a packed job.
+__device__ __forceinline__ bool molecule_inactive(const DPair& b, const unsigned char* active)
+{
+    return active != nullptr && __ldg(active + b.frag) == 0;
 }
 #endif
 

@@ -71,7 +71,7 @@ __global__ void k_lincomb(int n, Coef8 cf, double* C)
 
 static int grid_for(int n) { return std::min(1024, std::max(1, (n + 255) / 256)); }
 
-DeviceScf::DeviceScf(Job& job, const ScfSetup& setup, int nspin) : job_(job), K_(job.K()), nspin_(nspin)
+DeviceScf::DeviceScf(FockSource& job, const ScfSetup& setup, int nspin) : job_(job), K_(job.K()), nspin_(nspin)
 {
     st_ = job.stream();
     cublas_check(cublasCreate(&blas_), "create");
@@ -164,7 +164,7 @@ void DeviceScf::build(int mode, double dthr)
     if (nspin_ == 1) {
         double* out = mode == 2 ? dG_.p : G_.p;
         job_.fock_rhf_device_ex(src[0], out, mixed, dt);
-        fock_ms_ += job_.stats.ms;
+        fock_ms_ += job_.last_build_ms();
         if (mode == 2) axpby(1.0, Gr_[0].p, 1.0, dG_.p, G_.p);
         if (mode >= 1) {  // reference for the next incremental build
             cuda_check(cudaMemcpyAsync(Gr_[0].p, G_.p, sizeof(double) * K_ * K_, cudaMemcpyDeviceToDevice, st_), "copy");
@@ -176,7 +176,7 @@ void DeviceScf::build(int mode, double dthr)
         double* Ka = mode == 2 ? dK_[0].p : Kx_[0].p;
         double* Kb = mode == 2 ? dK_[1].p : Kx_[1].p;
         job_.fock_uhf_device_ex(src[0], src[1], J, Ka, Kb, mixed, dt);
-        fock_ms_ += job_.stats.ms;
+        fock_ms_ += job_.last_build_ms();
         if (mode == 2) {
             // reference J in Gr_[0], K_a in Gr_[1]; K_b kept in Kr_
             axpby(1.0, Gr_[0].p, 1.0, dG_.p, G_.p);

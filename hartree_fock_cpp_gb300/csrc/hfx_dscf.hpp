@@ -23,7 +23,7 @@ struct ScfControl {
 class DeviceScf {
 public:
     // nspin = 1 (RHF) or 2 (UHF)
-    DeviceScf(Job& job, const ScfSetup& setup, int nspin);
+    DeviceScf(FockSource& job, const ScfSetup& setup, int nspin);
     ~DeviceScf();
     DeviceScf(const DeviceScf&) = delete;
     DeviceScf& operator=(const DeviceScf&) = delete;
@@ -43,7 +43,7 @@ private:
     void error_and_energy();
     void diagonalise(const double* const* Fs, const int* nocc, double occ_factor);
 
-    Job& job_;
+    FockSource& job_;
     int K_, nspin_;
     cudaStream_t st_ = nullptr;
     cublasHandle_t blas_ = nullptr;

@@ -124,6 +124,67 @@ static double flops_per_prim(int la, int lb, int lc, int ld)
 
 Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
 {
+    frags_ = single_fragment(basis_);
+    init(opt);
+}
+
+Job::Job(const std::vector<Basis>& mols, const hfx_options& opt) : opt_(opt)
+{
+    if (mols.empty() || mols.size() > 65535) throw Error(HFX_ERR_INVALID, "packed job: 1..65535 molecules");
+    basis_ = concat_basis(mols, frags_);
+    init(opt);
+}
+
+void Job::set_active(const unsigned char* flags)
+{
+    if (!d_active_.p) throw Error(HFX_ERR_INVALID, "set_active: not a packed job");
+    cuda_check(cudaMemcpyAsync(d_active_.p, flags, frags_.count(), cudaMemcpyHostToDevice, stream_), "active flags");
+}
+
+Basis concat_basis(const std::vector<Basis>& mols, Fragments& fr)
+{
+    Basis out;
+    fr = Fragments{};
+    fr.sh.push_back(0);
+    fr.bf.push_back(0);
+    fr.pbase.push_back(0);
+    fr.moff.push_back(0);
+    fr.qoff.push_back(0);
+    for (const Basis& m : mols) {
+        const int atom0 = (int)out.atom_Z.size();
+        for (Shell sh : m.shells) {
+            sh.bf0 += out.K;
+            sh.atom += atom0;
+            out.shells.push_back(std::move(sh));
+        }
+        out.K += m.K;
+        out.atom_Z.insert(out.atom_Z.end(), m.atom_Z.begin(), m.atom_Z.end());
+        out.atom_xyz.insert(out.atom_xyz.end(), m.atom_xyz.begin(), m.atom_xyz.end());
+        const long long ns = (long long)m.shells.size();
+        fr.sh.push_back((int)out.shells.size());
+        fr.bf.push_back(out.K);
+        fr.pbase.push_back(fr.pbase.back() + (int)(ns * (ns + 1) / 2));
+        fr.moff.push_back(fr.moff.back() + (long long)m.K * m.K);
+        fr.qoff.push_back(fr.qoff.back() + (long long)m.K * (m.K + 1) / 2);
+    }
+    return out;
+}
+
+Fragments single_fragment(const Basis& b)
+{
+    Fragments fr;
+    const long long ns = (long long)b.shells.size();
+    fr.sh = {0, (int)ns};
+    fr.bf = {0, b.K};
+    fr.pbase = {0, (int)(ns * (ns + 1) / 2)};
+    fr.moff = {0, (long long)b.K * b.K};
+    fr.qoff = {0, (long long)b.K * (b.K + 1) / 2};
+    return fr;
+}
+
+void Job::init(const hfx_options& opt)
+{
+    opt_ = opt;
     if (opt_.screening_threshold == 0.0) opt_.screening_threshold = 1e-8;
     if (opt_.fp32_threshold == 0.0) opt_.fp32_threshold = 1e-7;
     device_ = opt_.device;
@@ -165,6 +226,21 @@ Job::Job(Basis b, const hfx_options& opt) : basis_(std::move(b)), opt_(opt)
     for (size_t p = 0; p < dpairs_host_.size(); ++p) dpairs_host_[p].qmax = qsh_[p];
     d_pairs_.upload(dpairs_host_, stream_);
     d_dsh_.alloc(std::max<size_t>(1, dpairs_host_.size()));
+    {
+        const int F = frags_.count();
+        std::vector<int> fk(F);
+        std::vector<long long> fm(F);
+        for (int f = 0; f < F; ++f) {
+            fk[f] = frags_.K(f);
+            fm[f] = frags_.moff[f];
+        }
+        d_fk_.upload(fk, stream_);
+        d_fmoff_.upload(fm, stream_);
+        if (F > 1) {
+            std::vector<unsigned char> on(F, 1);
+            d_active_.upload(on, stream_);
+        }
+    }
     build_jk_groups(false, gs_fp64_);
     if (mixed()) build_jk_groups(true, gs_mixed_);
     d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
@@ -231,15 +307,15 @@ const ClassTables& class_tables()
     return ct;
 }
 
-PairData build_pair_data(const Basis& basis)
+PairData build_pair_data(const Basis& basis, const Fragments& fr)
 {
     const ClassTables& ct = class_tables();
     const auto& sh = basis.shells;
-    int ns = (int)sh.size();
     PairData pd;
     std::vector<double> Ex, Ey, Ez;
-    for (int A = 0; A < ns; ++A)
-        for (int B = 0; B <= A; ++B) {
+    for (int f = 0; f < fr.count(); ++f)
+    for (int A = fr.sh[f]; A < fr.sh[f + 1]; ++A)
+        for (int B = fr.sh[f]; B <= A; ++B) {
             int s0 = A, s1 = B;
             if (sh[A].L < sh[B].L) std::swap(s0, s1);
             const Shell& S0 = sh[s0];
@@ -247,6 +323,7 @@ PairData build_pair_data(const Basis& basis)
             int l0 = S0.L, l1 = S1.L, L = l0 + l1;
             int n0 = ncart(l0), n1 = ncart(l1), H = nherm(L);
             HostPair hp;
+            hp.frag = f;
             hp.s0 = s0;
             hp.s1 = s1;
             hp.l0 = l0;
@@ -300,8 +377,8 @@ PairData build_pair_data(const Basis& basis)
                 }
             hp.npp = npp;
             DPair d{};
-            d.bf0 = S0.bf0;
-            d.bf1 = S1.bf0;
+            d.bf0 = S0.bf0 - fr.bf[f];
+            d.bf1 = S1.bf0 - fr.bf[f];
             d.l0 = l0;
             d.l1 = l1;
             d.pp0 = hp.pp0;
@@ -312,8 +389,13 @@ PairData build_pair_data(const Basis& basis)
             d.qmax = 0.0;
             d.rec_off = rec_off;
             d.pc = pc;
-            d.sh0 = s0;
-            d.sh1 = s1;
+            d.sh0 = s0 - fr.sh[f];
+            d.sh1 = s1 - fr.sh[f];
+            d.kdim = fr.K(f);
+            d.pbase = fr.pbase[f];
+            d.frag = f;
+            d.moff = fr.moff[f];
+            d.qoff = fr.qoff[f];
             pd.dpairs.push_back(d);
             pd.hpairs.push_back(hp);
         }
@@ -322,7 +404,7 @@ PairData build_pair_data(const Basis& basis)
 
 void Job::build_pairs()
 {
-    PairData pd = build_pair_data(basis_);
+    PairData pd = build_pair_data(basis_, frags_);
     hpairs_ = std::move(pd.hpairs);
     dpairs_host_ = pd.dpairs;
     d_pairs_.upload(pd.dpairs, stream_);
@@ -372,7 +454,7 @@ void Job::compute_schwarz()
     // BF-pair bounds sqrt((ab|ab)) and the per-pair maximum), tiered by the
     // shared-memory slice each class needs.
     const int np = (int)hpairs_.size();
-    size_t npair_bf = (size_t)basis_.K * (basis_.K + 1) / 2;
+    size_t npair_bf = (size_t)frags_.qoff.back();
     d_qbf_.alloc(npair_bf);
     d_qsh_.alloc(np);
     cuda_check(cudaMemsetAsync(d_qbf_.p, 0, npair_bf * sizeof(double), stream_), "memset");
@@ -437,29 +519,30 @@ void Job::compute_schwarz()
 
 void Job::schwarz_host(std::vector<double>& Q) const { Q = qbf_; }
 
-// Calls f(X, Y) for every unique shell-pair pair X >= Y with
-// Q_X Q_Y >= thr (all pairs if thr < 0), visiting only the survivors: the
-// pairs are scanned in decreasing Q order and the scan for X stops at the
-// first Q_Y below thr / Q_X.
+// Calls f(X, Y) for every unique shell-pair pair X >= Y of the same molecule
+// with Q_X Q_Y >= thr (all pairs if thr < 0), visiting only the survivors:
+// a molecule's pairs are scanned in decreasing Q order and the scan for X
+// stops at the first Q_Y below thr / Q_X.
 template <typename F>
 void Job::for_each_surviving_quartet(double thr, F&& f) const
 {
-    const int np = (int)hpairs_.size();
-    if (thr < 0.0) {
-        for (int X = 0; X < np; ++X)
-            for (int Y = 0; Y <= X; ++Y) f(X, Y);
-        return;
-    }
-    std::vector<int> order(np);
-    std::iota(order.begin(), order.end(), 0);
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return qsh_[a] > qsh_[b]; });
-    for (int X = 0; X < np; ++X) {
-        if (qsh_[X] <= 0.0) continue;
-        const double need = thr / qsh_[X];
-        for (int r = 0; r < np; ++r) {
-            const int Y = order[r];
-            if (qsh_[Y] < need) break;
-            if (Y <= X) f(X, Y);
+    for (int fr = 0; fr < frags_.count(); ++fr) {
+        const int p0 = frags_.pbase[fr], p1 = frags_.pbase[fr + 1];
+        if (thr < 0.0) {
+            for (int X = p0; X < p1; ++X)
+                for (int Y = p0; Y <= X; ++Y) f(X, Y);
+            continue;
+        }
+        std::vector<int> order(p1 - p0);
+        std::iota(order.begin(), order.end(), p0);
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return qsh_[a] > qsh_[b]; });
+        for (int X = p0; X < p1; ++X) {
+            if (qsh_[X] <= 0.0) continue;
+            const double need = thr / qsh_[X];
+            for (int Y : order) {
+                if (qsh_[Y] < need) break;
+                if (Y <= X) f(X, Y);
+            }
         }
     }
 }
@@ -722,11 +805,12 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
     const Task* tasks = gs.tasks.p;
     const double* Dsh = nullptr;
     int K = basis_.K;
+    const unsigned char* active = d_active_.p;
     if (dthr > 0.0 && !dpairs_host_.empty()) {
         const DPair* pr = d_pairs_.p;
         int np = (int)dpairs_host_.size();
         double* out = d_dsh_.p;
-        void* prm[] = {&pr, &np, &Dk, &Dk2, &K, &out};
+        void* prm[] = {&pr, &np, &Dk, &Dk2, &out};
         sk.kernel(0, density_blocks_spec(np), prm);
         Dsh = d_dsh_.p;
     }
@@ -745,13 +829,14 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
             next_aux = (next_aux + 1) % naux;
             if (g.fp32) {
                 SmallArgs<float> a{d_pairs_.p, d_rec32_.p, tasks + g.off, (int)g.n, d_boys32_.p,
-                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
+                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active};
                 cuda_check(small_spec_f32(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
             } else {
                 SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys_.p,
-                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr};
+                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr,
+                                    active};
                 cuda_check(small_spec_f64(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
@@ -762,14 +847,14 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                   tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
-                                  Dsh, dthr};
+                                  Dsh, dthr, nullptr, nullptr, active};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                    tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
-                                   Dsh, dthr};
+                                   Dsh, dthr, nullptr, nullptr, active};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             }
@@ -808,7 +893,7 @@ cudaGraphExec_t Job::graph_for(int nk, bool mixed_plan, double dthr)
     GraphEntry& g = graphs_[std::make_tuple(nk, mixed_plan, dthr)];
     if (g.exec) return g.exec;
     if (g.eager_runs < 1) return nullptr;   // the first build of a variant runs eagerly
-    const size_t n = (size_t)basis_.K * basis_.K;
+    const size_t n = (size_t)nmat();
     d_gin_.alloc(n);
     d_gout_.alloc(n);
     if (nk == 2) {
@@ -832,24 +917,35 @@ void Job::clear_graphs()
     graphs_.clear();
 }
 
+int Job::max_fragment_K() const
+{
+    int m = 0;
+    for (int f = 0; f < frags_.count(); ++f) m = std::max(m, frags_.K(f));
+    return m;
+}
+
+void Job::enqueue_finish_rhf(OpSink& sk, const double* Jacc, const double* Kacc, double* dG)
+{
+    const int* fk = d_fk_.p;
+    const long long* fm = d_fmoff_.p;
+    const unsigned char* act = d_active_.p;
+    void* prm[] = {&Jacc, &Kacc, &dG, &fk, &fm, &act};
+    sk.kernel(0, finish_rhf_spec(max_fragment_K(), frags_.count()), prm);
+}
+
 void Job::enqueue_rhf(OpSink& sk, const double* dP, double* dG, bool mixed_plan, double dthr)
 {
-    int K = basis_.K;
-    const size_t n = (size_t)K * K;
+    const size_t n = (size_t)nmat();
     sk.zero(0, d_J_.p, n * sizeof(double));
     sk.zero(0, d_K_.p, n * sizeof(double));
     launch_jk(sk, 1, dP, dP, nullptr, d_J_.p, d_K_.p, nullptr, nullptr, mixed_plan, dthr);
-    const double* jp = d_J_.p;
-    const double* kp = d_K_.p;
-    void* prm[] = {&jp, &kp, &dG, &K};
-    sk.kernel(0, finish_rhf_spec(K), prm);
+    enqueue_finish_rhf(sk, d_J_.p, d_K_.p, dG);
 }
 
 void Job::enqueue_uhf(OpSink& sk, const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb,
                       bool mixed_plan, double dthr)
 {
-    int K = basis_.K;
-    int n = K * K;
+    long long n = nmat();
     sk.zero(0, d_J_.p, (size_t)n * sizeof(double));
     sk.zero(0, d_K_.p, (size_t)n * sizeof(double));
     sk.zero(0, d_K2_.p, (size_t)n * sizeof(double));
@@ -860,15 +956,17 @@ void Job::enqueue_uhf(OpSink& sk, const double* dPa, const double* dPb, double* 
     const double* jp = d_J_.p;
     const double* kp = d_K_.p;
     const double* k2 = d_K2_.p;
-    void* prm[] = {&jp, &kp, &k2, &dJ, &dKa, &dKb, &K};
-    sk.kernel(0, finish_uhf_spec(K), prm);
+    const int* fk = d_fk_.p;
+    const long long* fm = d_fmoff_.p;
+    const unsigned char* act = d_active_.p;
+    void* prm[] = {&jp, &kp, &k2, &dJ, &dKa, &dKb, &fk, &fm, &act};
+    sk.kernel(0, finish_uhf_spec(max_fragment_K(), frags_.count()), prm);
 }
 
 void Job::fock_rhf_device_ex(const double* dP, double* dG, bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    const int K = basis_.K;
-    const size_t n = (size_t)K * K;
+    const size_t n = (size_t)nmat();
     d_J_.alloc(n);
     d_K_.alloc(n);
     cudaGraphExec_t ge = graph_for(1, mixed_plan, dthr);
@@ -903,10 +1001,7 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
     cuda_check(cudaEventRecord(evk0_, stream_), "event");
     launch_jk(sk, 1, dP, dP, nullptr, Jacc, Kacc, nullptr, counters, mixed(), 0.0);
     cuda_check(cudaEventRecord(evk1_, stream_), "event");
-    const double* jp = Jacc;
-    const double* kp = Kacc;
-    void* prm[] = {&jp, &kp, &dG, &K};
-    sk.kernel(0, finish_rhf_spec(K), prm);
+    enqueue_finish_rhf(sk, Jacc, Kacc, dG);
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats((int)plan(mixed()).groups.size() + 1);
@@ -915,7 +1010,7 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
 double Job::autotune_fp32_threshold(const double* P, double target_dE, double* dE_out, double* ms64, double* msmx)
 {
     const int K = basis_.K;
-    const size_t n = (size_t)K * K;
+    const size_t n = (size_t)nmat();
     std::vector<double> G64(n), Gm(n);
     fock_rhf_ex(P, G64.data(), false, 0.0);
     fock_rhf_ex(P, G64.data(), false, 0.0);
@@ -965,8 +1060,7 @@ void Job::fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, d
                              bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    const int K = basis_.K;
-    const size_t n = (size_t)K * K;
+    const size_t n = (size_t)nmat();
     d_J_.alloc(n);
     d_K_.alloc(n);
     d_K2_.alloc(n);
@@ -1000,7 +1094,7 @@ void Job::fock_rhf(const double* P, double* G) { fock_rhf_ex(P, G, mixed(), 0.0)
 void Job::fock_rhf_ex(const double* P, double* G, bool mixed_plan, double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    size_t n = (size_t)basis_.K * basis_.K;
+    size_t n = (size_t)nmat();
     d_D_.alloc(n);
     d_out1_.alloc(n);
     cuda_check(cudaMemcpyAsync(d_D_.p, P, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D");
@@ -1018,7 +1112,7 @@ void Job::fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka,
                       double dthr)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
-    size_t n = (size_t)basis_.K * basis_.K;
+    size_t n = (size_t)nmat();
     d_D_.alloc(n);
     d_D2_.alloc(n);
     d_out1_.alloc(n);
@@ -1036,6 +1130,7 @@ void Job::fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka,
 void Job::eri_unique(double thr, double* out)
 {
     cuda_check(cudaSetDevice(device_), "cudaSetDevice");
+    if (frags_.count() != 1) throw Error(HFX_ERR_INVALID, "eri_unique: packed job");
     size_t P = (size_t)basis_.K * (basis_.K + 1) / 2;
     size_t nq = P * (P + 1) / 2;
     DevBuf<double> d_out;

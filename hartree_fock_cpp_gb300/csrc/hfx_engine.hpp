@@ -17,10 +17,12 @@ namespace hfx {
 size_t generic_smem_bytes(int maxacc, int maxw, int maxr);
 cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
                            cudaStream_t st);
-KernelSpec finish_rhf_spec(int K);   // k_finish_rhf(Jacc, Kacc, G, K)
-KernelSpec finish_uhf_spec(int K);   // k_finish_uhf(Jacc, Ka, Kb, J, Kao, Kbo, K)
-KernelSpec add_spec(int n);          // k_add(A, B, C, n)
-KernelSpec density_blocks_spec(int npairs);   // k_density_blocks(pairs, npairs, D1, D2, K, Dsh)
+// symmetrisation of packed accumulators: one grid row (blockIdx.y) per
+// molecule, Kmax = the largest molecule's K
+KernelSpec finish_rhf_spec(int Kmax, int nfrag);   // k_finish_rhf(Jacc, Kacc, G, fk, fmoff, active)
+KernelSpec finish_uhf_spec(int Kmax, int nfrag);   // k_finish_uhf(Jacc, Ka, Kb, J, Kao, Kbo, fk, fmoff, active)
+KernelSpec add_spec(long long n);    // k_add(A, B, C, n)
+KernelSpec density_blocks_spec(int npairs);   // k_density_blocks(pairs, npairs, D1, D2, Dsh)
 cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<double>)
 cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<float>)
 cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s);
@@ -71,7 +73,8 @@ struct DevBuf {
 };
 
 struct HostPair {
-    int s0, s1;       // shells (s0 has the higher L)
+    int frag;         // molecule of a packed job
+    int s0, s1;       // shells (s0 has the higher L), indices in the concatenated basis
     int l0, l1;
     int npp;
     long long e_off;
@@ -107,7 +110,24 @@ struct LaunchGroup {
     size_t off, n;       // task range in the concatenated list
     double flops, prims;
 };
-PairData build_pair_data(const Basis& b);
+// Molecules of a packed job (one entry for a plain job): molecule f owns
+// shells [sh[f], sh[f+1]) and basis functions [bf[f], bf[f+1]) of the
+// concatenated basis, shell pairs [pbase[f], pbase[f+1]), the K_f x K_f
+// block at moff[f] of every packed matrix buffer and the BF-pair bounds at
+// qoff[f].
+struct Fragments {
+    std::vector<int> sh, bf, pbase;
+    std::vector<long long> moff, qoff;
+    int count() const { return (int)sh.size() - 1; }
+    int K(int f) const { return bf[f + 1] - bf[f]; }
+    long long nmat() const { return moff.back(); }
+};
+// Concatenate molecules' bases (shell bf0 shifted to the concatenated order)
+// and describe the blocks.
+Basis concat_basis(const std::vector<Basis>& mols, Fragments& fr);
+Fragments single_fragment(const Basis& b);
+
+PairData build_pair_data(const Basis& b, const Fragments& fr);
 
 // The launch plan of one precision mode.
 struct GroupSet {
@@ -165,12 +185,36 @@ private:
     std::vector<std::vector<cudaGraphNode_t>> deps_;   // per lane: the nodes its next node depends on
 };
 
-class Job {
+// What the device SCF needs from a Fock builder: a job of its own, or one
+// molecule's share of a packed job (hfx_batch.cpp).  Builds are synchronous
+// with respect to stream().
+class FockSource {
+public:
+    virtual ~FockSource() = default;
+    virtual int K() const = 0;
+    virtual cudaStream_t stream() const = 0;
+    virtual bool mixed() const = 0;
+    virtual void fock_rhf_device_ex(const double* dP, double* dG, bool mixed, double dthr) = 0;
+    virtual void fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb,
+                                    bool mixed, double dthr) = 0;
+    virtual double last_build_ms() const = 0;   // device time of the last build
+};
+
+class Job final : public FockSource {
 public:
     Job(Basis b, const hfx_options& opt);
+    // Packed job over several molecules: shell pairs and quartets never mix
+    // molecules, and every Fock build works on packed buffers holding each
+    // molecule's K_f x K_f matrices back to back (the blocks of fragments()).
+    Job(const std::vector<Basis>& mols, const hfx_options& opt);
     ~Job();
 
-    int K() const { return basis_.K; }
+    const Fragments& fragments() const { return frags_; }
+    long long nmat() const { return frags_.nmat(); }
+    // packed jobs: molecules whose flag is 0 are skipped by the next builds
+    void set_active(const unsigned char* flags);
+
+    int K() const override { return basis_.K; }
     int device() const { return device_; }
     const Basis& basis() const { return basis_; }
 
@@ -180,12 +224,13 @@ public:
     // Builds with an explicit precision plan (mixed = false: every quartet in
     // FP64) and density-weighted screening threshold (0: none; used by the
     // incremental builds of the mixed-precision SCF).
-    void fock_rhf_device_ex(const double* dP, double* dG, bool mixed, double dthr);
+    void fock_rhf_device_ex(const double* dP, double* dG, bool mixed, double dthr) override;
     void fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb, bool mixed,
-                            double dthr);
+                            double dthr) override;
+    double last_build_ms() const override { return stats.ms; }
     void fock_rhf_ex(const double* P, double* G, bool mixed, double dthr);
     void fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, bool mixed, double dthr);
-    bool mixed() const { return opt_.precision == HFX_PREC_MIXED; }
+    bool mixed() const override { return opt_.precision == HFX_PREC_MIXED; }
     double fp32_threshold() const { return opt_.fp32_threshold; }
     // Pick the FP32 threshold: for each candidate (largest first) build G in
     // mixed precision at density P and keep the largest tau whose energy
@@ -204,9 +249,10 @@ public:
     void eri_unique(double thr, double* out);
 
     hfx_build_stats stats{};
-    cudaStream_t stream() const { return stream_; }
+    cudaStream_t stream() const override { return stream_; }
 
 private:
+    void init(const hfx_options& opt);
     void build_pairs();
     void compute_schwarz();
     void build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops = nullptr,
@@ -231,6 +277,8 @@ private:
     const GroupSet& plan(bool mixed_plan) const { return mixed_plan && mixed() ? gs_mixed_ : gs_fp64_; }
     void record_stats_plan(int launches, const GroupSet& gs);
     StreamSink stream_sink() { return StreamSink(stream_, aux_, fork_ev_, aux_ev_); }
+    int max_fragment_K() const;
+    void enqueue_finish_rhf(OpSink& sk, const double* Jacc, const double* Kacc, double* dG);
     void enqueue_rhf(OpSink& sk, const double* dP, double* dG, bool mixed_plan, double dthr);
     void enqueue_uhf(OpSink& sk, const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb, bool mixed_plan,
                      double dthr);
@@ -243,6 +291,10 @@ private:
     std::map<std::tuple<int, bool, double>, GraphEntry> graphs_;
     bool no_graphs_ = false;
     DevBuf<double> d_gin_, d_gin2_, d_gout_, d_gout2_, d_gout3_;
+    Fragments frags_;
+    DevBuf<int> d_fk_;              // per molecule K_f
+    DevBuf<long long> d_fmoff_;     // per molecule matrix offset
+    DevBuf<unsigned char> d_active_;   // packed jobs: per molecule build flag
 
     std::vector<HostPair> hpairs_;
     GroupSet gs_fp64_, gs_mixed_;

@@ -256,40 +256,49 @@ __global__ void __launch_bounds__(128) k_quartet_generic(LaunchArgs a, int maxac
     }
 }
 
-// G = (Jacc + Jacc^T)/4 - 1/2 (Kacc + Kacc^T)/8   (RHF, linalg.hpp:100-129)
-__global__ void k_finish_rhf(const double* Jacc, const double* Kacc, double* G, int K)
+// G = (Jacc + Jacc^T)/4 - 1/2 (Kacc + Kacc^T)/8   (RHF, linalg.hpp:100-129),
+// per molecule block of the packed buffers (blockIdx.y = molecule); blocks of
+// molecules switched off for this build (active[f] == 0) are left untouched
+__global__ void k_finish_rhf(const double* Jacc, const double* Kacc, double* G, const int* fk, const long long* fmoff,
+                             const unsigned char* active)
 {
-    int n = K * K;
+    if (active && !active[blockIdx.y]) return;
+    const int K = fk[blockIdx.y];
+    const long long o = fmoff[blockIdx.y];
+    const int n = K * K;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         int i = e / K, j = e - i * K;
-        double J = 0.25 * (Jacc[e] + Jacc[j * K + i]);
-        double X = 0.125 * (Kacc[e] + Kacc[j * K + i]);
-        G[e] = J - 0.5 * X;
+        double J = 0.25 * (Jacc[o + e] + Jacc[o + j * K + i]);
+        double X = 0.125 * (Kacc[o + e] + Kacc[o + j * K + i]);
+        G[o + e] = J - 0.5 * X;
     }
 }
 
 // J = (Jacc + Jacc^T)/4, K = (Kacc + Kacc^T)/8  (UHF, linalg.hpp:215-296)
 __global__ void k_finish_uhf(const double* Jacc, const double* Ka, const double* Kb, double* J, double* Kao,
-                             double* Kbo, int K)
+                             double* Kbo, const int* fk, const long long* fmoff, const unsigned char* active)
 {
-    int n = K * K;
+    if (active && !active[blockIdx.y]) return;
+    const int K = fk[blockIdx.y];
+    const long long o = fmoff[blockIdx.y];
+    const int n = K * K;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         int i = e / K, j = e - i * K;
-        J[e] = 0.25 * (Jacc[e] + Jacc[j * K + i]);
-        Kao[e] = 0.125 * (Ka[e] + Ka[j * K + i]);
-        Kbo[e] = 0.125 * (Kb[e] + Kb[j * K + i]);
+        J[o + e] = 0.25 * (Jacc[o + e] + Jacc[o + j * K + i]);
+        Kao[o + e] = 0.125 * (Ka[o + e] + Ka[o + j * K + i]);
+        Kbo[o + e] = 0.125 * (Kb[o + e] + Kb[o + j * K + i]);
     }
 }
 
-__global__ void k_add(const double* A, const double* B, double* C, int n)
+__global__ void k_add(const double* A, const double* B, double* C, long long n)
 {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) C[e] = A[e] + B[e];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        C[e] = A[e] + B[e];
 }
 
 // Dsh[p] = max over the (A, B) block of max(|D1|, |D2|), for every shell pair
 // p (D2 may be null); the density-weighted screening of incremental builds.
-__global__ void k_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, int K,
-                                 double* Dsh)
+__global__ void k_density_blocks(const DPair* pairs, int npairs, const double* D1, const double* D2, double* Dsh)
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
@@ -298,7 +307,7 @@ __global__ void k_density_blocks(const DPair* pairs, int npairs, const double* D
     double m = 0.0;
     for (int a = 0; a < n0; ++a)
         for (int b = 0; b < n1; ++b) {
-            long long e = (long long)(pr.bf0 + a) * K + pr.bf1 + b;
+            long long e = pr.moff + (long long)(pr.bf0 + a) * pr.kdim + pr.bf1 + b;
             m = fmax(m, fabs(D1[e]));
             if (D2) m = fmax(m, fabs(D2[e]));
         }
@@ -356,19 +365,25 @@ cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, in
     return go(k_quartet_generic<MODE_JK, 1>);
 }
 
-// Grid-stride elementwise kernels: 256 threads, at most 1024 CTAs.
-static KernelSpec elementwise_spec(const void* func, long long n)
+// Grid-stride elementwise kernels: 256 threads, at most 1024 CTAs per grid row.
+static KernelSpec elementwise_spec(const void* func, long long n, int rows)
 {
     KernelSpec s;
     s.func = func;
     long long grid = (n + 255) / 256;
-    s.grid = dim3((unsigned)std::max(1LL, std::min(grid, 1024LL)));
+    s.grid = dim3((unsigned)std::max(1LL, std::min(grid, 1024LL)), (unsigned)std::max(1, rows));
     s.block = dim3(256);
     return s;
 }
 
-KernelSpec finish_rhf_spec(int K) { return elementwise_spec((const void*)k_finish_rhf, (long long)K * K); }
-KernelSpec finish_uhf_spec(int K) { return elementwise_spec((const void*)k_finish_uhf, (long long)K * K); }
-KernelSpec add_spec(int n) { return elementwise_spec((const void*)k_add, n); }
+KernelSpec finish_rhf_spec(int Kmax, int nfrag)
+{
+    return elementwise_spec((const void*)k_finish_rhf, (long long)Kmax * Kmax, nfrag);
+}
+KernelSpec finish_uhf_spec(int Kmax, int nfrag)
+{
+    return elementwise_spec((const void*)k_finish_uhf, (long long)Kmax * Kmax, nfrag);
+}
+KernelSpec add_spec(long long n) { return elementwise_spec((const void*)k_add, n, 1); }
 
 }  // namespace hfx

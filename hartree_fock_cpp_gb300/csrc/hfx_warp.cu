@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         const Task task = a.tasks[tk];
         const DPair bra = a.pairs[task.bra];
         const DPair ket = a.pairs[task.ket];
+        if (molecule_inactive(bra, a.active)) continue;
         if (density_negligible(bra, ket, a.Dsh, a.dthr)) continue;
         const PairClassTab cb = a.pct[bra.pc];
         const PairClassTab ck = a.pct[ket.pc];
@@ -366,15 +367,22 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 if (bra.same && ia < ib) continue;
                 const double v = (double)acc[e];
                 const double qv = sqrt(v > 0.0 ? v : 0.0);
-                a.Qout_bf[wpidx(bra.bf0 + ia, bra.bf1 + ib)] = qv;
+                a.Qout_bf[bra.qoff + wpidx(bra.bf0 + ia, bra.bf1 + ib)] = qv;
                 atomicMax(a.Qout_sh + task.bra, (unsigned long long)__double_as_longlong(qv));
             }
             __syncwarp();
             continue;
         }
 
-        // digestion (FP64)
-        const int K = a.K;
+        // digestion (FP64), into the bra pair's molecule's matrices
+        const int K = bra.kdim;
+        const double* __restrict__ Qbf = a.Qbf + bra.qoff;
+        const double* __restrict__ Dj = a.Dj + bra.moff;
+        const double* __restrict__ Dk = a.Dk + bra.moff;
+        const double* __restrict__ Dk2 = a.Dk2 + (NK == 2 ? bra.moff : 0);
+        double* J = a.J + bra.moff;
+        double* Kx = a.Kx + bra.moff;
+        double* Kx2 = a.Kx2 + (NK == 2 ? bra.moff : 0);
         for (int e = lane; e < nout; e += 32) {
             const int ab = e / ncd, cd = e - ab * ncd;
             const int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
@@ -383,19 +391,19 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             if (ket.same && ic < id) continue;
             const long long pij = wpidx(i, j), pkl = wpidx(k, l);
             if (task.bra == task.ket && pij < pkl) continue;
-            if (a.thr >= 0.0 && __ldg(a.Qbf + pij) * __ldg(a.Qbf + pkl) < a.thr) continue;
+            if (a.thr >= 0.0 && __ldg(Qbf + pij) * __ldg(Qbf + pkl) < a.thr) continue;
             double v = (double)acc[e] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
-            atomicAdd(a.J + (long long)i * K + j, __ldg(a.Dj + (long long)k * K + l) * v);
-            atomicAdd(a.J + (long long)k * K + l, __ldg(a.Dj + (long long)i * K + j) * v);
-            atomicAdd(a.Kx + (long long)i * K + k, __ldg(a.Dk + (long long)j * K + l) * v);
-            atomicAdd(a.Kx + (long long)j * K + l, __ldg(a.Dk + (long long)i * K + k) * v);
-            atomicAdd(a.Kx + (long long)i * K + l, __ldg(a.Dk + (long long)j * K + k) * v);
-            atomicAdd(a.Kx + (long long)j * K + k, __ldg(a.Dk + (long long)i * K + l) * v);
+            atomicAdd(J + (long long)i * K + j, __ldg(Dj + (long long)k * K + l) * v);
+            atomicAdd(J + (long long)k * K + l, __ldg(Dj + (long long)i * K + j) * v);
+            atomicAdd(Kx + (long long)i * K + k, __ldg(Dk + (long long)j * K + l) * v);
+            atomicAdd(Kx + (long long)j * K + l, __ldg(Dk + (long long)i * K + k) * v);
+            atomicAdd(Kx + (long long)i * K + l, __ldg(Dk + (long long)j * K + k) * v);
+            atomicAdd(Kx + (long long)j * K + k, __ldg(Dk + (long long)i * K + l) * v);
             if (NK == 2) {
-                atomicAdd(a.Kx2 + (long long)i * K + k, __ldg(a.Dk2 + (long long)j * K + l) * v);
-                atomicAdd(a.Kx2 + (long long)j * K + l, __ldg(a.Dk2 + (long long)i * K + k) * v);
-                atomicAdd(a.Kx2 + (long long)i * K + l, __ldg(a.Dk2 + (long long)j * K + k) * v);
-                atomicAdd(a.Kx2 + (long long)j * K + k, __ldg(a.Dk2 + (long long)i * K + l) * v);
+                atomicAdd(Kx2 + (long long)i * K + k, __ldg(Dk2 + (long long)j * K + l) * v);
+                atomicAdd(Kx2 + (long long)j * K + l, __ldg(Dk2 + (long long)i * K + k) * v);
+                atomicAdd(Kx2 + (long long)i * K + l, __ldg(Dk2 + (long long)j * K + k) * v);
+                atomicAdd(Kx2 + (long long)j * K + k, __ldg(Dk2 + (long long)i * K + l) * v);
             }
         }
         __syncwarp();

@@ -313,6 +313,40 @@ hfx_status hfx_server_density(hfx_server *server, long long id, double *Pa, doub
 hfx_status hfx_server_stats(hfx_server *server, hfx_server_stats_t *stats);
 hfx_status hfx_server_destroy(hfx_server *server);
 
+/* ---- lockstep batched SCF (packed Fock builds) ---------------------------
+ * Replaces the sequential scan drivers run_bl_scan (run.hpp:300-423) and
+ * run_dissociation (run.hpp:498-577), which solve one geometry after another.
+ * All n molecules (any mix of sizes and basis sets) share one packed job and
+ * iterate in lockstep: each SCF cycle is ONE Fock build over every molecule
+ * still iterating (one launch per quartet class over all molecules'
+ * quartets, replayed as a CUDA graph), each molecule's O(K^3) SCF steps run
+ * on its own stream.  Every molecule starts from the zero density (the
+ * reference's sequential scan warm-starts from the previous geometry).
+ * One method per batch; UHF takes per-molecule n_alpha[i], n_beta[i].
+ * results[i] gets molecule i's result.  HFX_ERR_NOT_CONVERGED if some
+ * molecule did not converge (every result still filled); any other failure
+ * returns the first failing molecule's status. */
+typedef struct {
+    int method;              /* 0 RHF, 1 UHF */
+    int max_parallel;        /* molecules iterating at once (0: all, at most 256) */
+    int reserved[6];
+} hfx_batch_options;
+
+typedef struct {
+    double seconds;          /* wall time of the whole batch, setup included */
+    double setup_seconds;    /* bases + packed job (pair data, Schwarz, plans) */
+    int cycles;              /* packed Fock builds run */
+    int molecules;
+    double build_ms;         /* device time of all packed builds */
+    double quartets;         /* surviving shell quartets of one packed build, all molecules */
+    double flops_fp64;       /* algorithmic FP64 flops of that build */
+    double reserved[5];
+} hfx_batch_stats;
+
+hfx_status hfx_batch_scf(const hfx_molecule *mols, int n, const int *n_alpha, const int *n_beta,
+                         const hfx_scf_options *scf, const hfx_batch_options *opt, hfx_scf_result *results,
+                         hfx_batch_stats *stats);
+
 /* Last error message of the calling thread (empty if none). */
 hfx_status hfx_last_error(char *buf, size_t n);
 
