@@ -48,6 +48,24 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws):
+    """The largest per-rank value over all ranks (the slowest rank's time);
+    NCCL reduces on the GPU, gloo on the CPU."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, t_max, ws):
+    """Units all ranks processed (each rank the same count) over the slowest rank's time."""
+    return ws * units_per_rank / t_max
+
+
 class Clocks:
     """nvidia-smi sampling of SM clocks and throttle reasons."""
 
@@ -229,12 +247,8 @@ def run_engine(args):
         iters, builds = it, nb
     clk = clocks.stop()
     torch.cuda.synchronize()
-    t_total = sum(lat) / 1e3
-    if ws > 1:
-        tt = torch.tensor([t_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = ws * args.steps / t_total
+    t_total = max_over_ranks(sum(lat) / 1e3, ws)
+    value = whole_job_rate(args.steps, t_total, ws)
 
     # ---- Fock builds/s (device-pointer build) and the kernel roofline --------
     rng = np.random.default_rng(0)
@@ -300,6 +314,11 @@ def run_engine(args):
     if args.serve_jobs > 0:
         served = serve_section(H, W, args.serve_jobs, local)
 
+    # ---- batched radial scans: packed lockstep SCF vs one-at-a-time FP64 -----
+    scans = None
+    if args.scan_points > 0:
+        scans = scan_section(H, W, args.scan_points)
+
     # ---- e2e: through hfx_rhf_diis with host buffers -------------------------
     e2e_lat = []
     r = None
@@ -309,11 +328,7 @@ def run_engine(args):
         dt = time.perf_counter() - t0
         if k > 0:
             e2e_lat.append(dt)
-    e2e_t = float(np.mean(e2e_lat))
-    if ws > 1:
-        tt = torch.tensor([e2e_t], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = max_over_ranks(float(np.mean(e2e_lat)), ws)
     m = H._lib.MoleculeArgs(cfg, basis)
     npp = ctypes.c_int()
     npr = ctypes.c_int()
@@ -344,11 +359,12 @@ def run_engine(args):
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},
         "mixed_precision": mixed,
         "served_stream": served,
+        "batched_scans": scans,
         "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP64 FMA-loop peak of this GPU (hfx_measure_peaks, same run)",
                      "flops_per_launch": flops, "kernel_ms": kernel_ms, "fp32_peak_tflops": fp32_peak / 1e3},
-        "e2e": {"value": 1.0 / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": whole_job_rate(1, e2e_t, ws), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(args.steps * builds * s["launches"]),
         "clocks": clk,
     }
@@ -419,6 +435,36 @@ def serve_section(H, W, n_jobs, device, rate_factor=2.0, tau=0.03, max_it=60, se
                              "max_abs_dE_vs_fp64": float(max(dE)) if dE else None}}
 
 
+def scan_section(H, W, n_each, n_seq=4):
+    """NaCl (Na-Cl 3.5..7.0 bohr) and water symmetric-stretch (O-H 1.4..3.0
+    bohr, 104.5 deg) scans, cc-pVTZ, FP64: n_each evenly spaced points of each
+    64-point scan solved at once by the lockstep batched SCF (one packed Fock
+    build per cycle, every point from the zero density), against the plain
+    FP64 GPU path one point at a time on n_seq of the same points."""
+    step = max(1, 64 // n_each)
+    nacl = W.nacl_scan(64)[::step][:n_each]
+    wat = W.water_scan(64)[::step][:n_each]
+    mols = [(c, "cc-pVTZ") for c in nacl] + [(c, "cc-pVTZ") for c in wat]
+    t0 = time.perf_counter()
+    res, st = H.batch_scf(mols, max_it=200)
+    T_b = time.perf_counter() - t0
+    ok = sum(1 for r in res if r["converged"])
+    pick = [0, len(nacl) - 1, len(nacl), len(mols) - 1][:n_seq]
+    t0 = time.perf_counter()
+    seq = [H.rhf_diis(mols[i][0], "cc-pVTZ", max_it=200) for i in pick]
+    T_s = time.perf_counter() - t0
+    dE = [abs(a["E_tot"] - res[i]["E_tot"]) for i, a in zip(pick, seq)]
+    dI = [abs(a["iterations"] - res[i]["iterations"]) for i, a in zip(pick, seq)]
+    return {"workload": "%d NaCl + %d water cc-pVTZ scan points (every %d-th of 64 each), RHF FP64, K=78/65"
+                        % (len(nacl), len(wat), step),
+            "batched": {"solves_per_s": ok / T_b, "seconds": T_b, "setup_s": st["setup_seconds"],
+                        "cycles": st["cycles"], "packed_build_ms_mean": st["build_ms"] / max(1, st["cycles"]),
+                        "converged": ok, "molecules": len(mols)},
+            "one_at_a_time_fp64": {"solves_per_s": len(pick) / T_s, "sample_points": len(pick), "seconds": T_s},
+            "speedup": (ok / T_b) / (len(pick) / T_s),
+            "max_abs_dE_vs_single": float(max(dE)), "max_iteration_diff": int(max(dI))}
+
+
 def run_fock_only(args):
     """Small fixed case for profilers: one job, a few device Fock builds."""
     import torch
@@ -449,6 +495,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision section")
     ap.add_argument("--serve-jobs", type=int, default=12, help="served-stream sample size (0: skip)")
+    ap.add_argument("--scan-points", type=int, default=16,
+                    help="batched-scan section: points of each 64-point scan (64: the full 64+64; 0: skip)")
     ap.add_argument("--fock-only", action="store_true",
                     help="profiling case: job setup + --builds device Fock builds of --molecule/--basis")
     ap.add_argument("--molecule", default="benzene", choices=["water", "benzene", "n_decane"])

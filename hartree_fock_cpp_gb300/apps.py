@@ -13,10 +13,11 @@ plain K x K tables.
 
 eri_hardware "GPU" runs the engine; "CPU" names the reference's own
 stored-tensor path, which this library does not contain, and is rejected.
-bl_scan --batched submits every scan geometry at once to the request server
-(all points' Fock builds in flight together, cold-start densities); without it
-the scan runs point after point with the previous density as the initial
-guess, as run_bl_scan does (run.hpp:329-368).
+bl_scan --batched solves every scan geometry at once on one packed job
+(batch_scf: one Fock build per SCF cycle over all points still iterating,
+cold-start densities); without it the scan runs point after point with the
+previous density as the initial guess, as run_bl_scan does
+(run.hpp:329-368).  dissociation solves the free atoms as one UHF batch.
 """
 import argparse
 import collections
@@ -27,7 +28,7 @@ import time
 
 import numpy as np
 
-from . import rhf_diis, uhf_diis, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError
+from . import batch_scf, rhf_diis, uhf_diis, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError
 
 ANGLE = math.pi / 180.0
 
@@ -179,28 +180,26 @@ def scan_geometry(opt, r):
     return cfg
 
 
-def run_bl_scan(opt, batched=False, max_active=16):
-    """run.hpp:300-423; batched=True runs every point concurrently through the
-    request server."""
+def run_bl_scan(opt, batched=False, max_parallel=0):
+    """run.hpp:300-423.  batched=True solves every point at once on one packed
+    job (batch_scf: one Fock build per SCF cycle over all points still
+    iterating, each point from the zero density) instead of one after the
+    other with warm starts; homo/lumo are then not reported (NaN)."""
     t0 = time.time()
     dist = scan_distances(opt["distances"])
     E, homo, lumo, its = [], [], [], []
     K = None
     if batched:
-        from .server import Server
-        with Server(max_active=max_active, precision=opt["precision"], fp32_threshold=opt["fp32_threshold"]) as srv:
-            ids = [srv.submit(scan_geometry(opt, r), opt["basis"], charge=opt["charge"], epsilon=opt["epsilon"],
-                              max_it=opt["max_it"], basis_path=opt["basis_path"]) for r in dist]
-            srv.drain(0)
-            for i in ids:
-                inf = srv.poll(i)
-                if inf["state"] != "done":
-                    raise HfxError(inf["status"], inf["message"])
-                E.append(inf["E_tot"])
-                its.append(inf["iterations"])
-                homo.append(float("nan"))
-                lumo.append(float("nan"))
-                K = inf["K"]
+        kw = _scf_kw(opt)
+        kw.pop("eri_device")
+        res, _ = batch_scf([(scan_geometry(opt, r), opt["basis"]) for r in dist], max_parallel=max_parallel,
+                           param_path=opt["basis_path"], **kw)
+        for r in res:
+            E.append(r["E_tot"])
+            its.append(r["iterations"])
+            homo.append(float("nan"))
+            lumo.append(float("nan"))
+            K = r["K"]
     else:
         P = None
         for r in dist:
@@ -235,14 +234,17 @@ def run_dissociation(opt):
         raise RuntimeError("dissociation energy only support RHF molecules")
     mol = rhf_diis(opt["config"], opt["basis"], opt["basis_path"], **_scf_kw(opt))
     counts = collections.Counter(s for s, _ in opt["config"])
-    atom_E = {}
     for sym in sorted(counts):
         if sym not in ATOM_SPIN:
             raise RuntimeError("Spin occupancy not implemented for atom: " + sym)
-        kw = _scf_kw(opt)
-        kw["charge"] = 0
-        a = uhf_diis([(sym, (0.0, 0.0, 0.0))], opt["basis"], opt["basis_path"], spin_occ=ATOM_SPIN[sym], **kw)
-        atom_E[sym] = a["E_tot"]
+    # the free atoms as one UHF batch on a packed job
+    kw = _scf_kw(opt)
+    kw.pop("eri_device")
+    kw["charge"] = 0
+    atoms = sorted(counts)
+    res, _ = batch_scf([([(sym, (0.0, 0.0, 0.0))], opt["basis"]) for sym in atoms], method="UHF",
+                       spins=[ATOM_SPIN[sym] for sym in atoms], param_path=opt["basis_path"], **kw)
+    atom_E = {sym: r["E_tot"] for sym, r in zip(atoms, res)}
     Ed = sum(counts[s] * atom_E[s] for s in counts) - mol["E_tot"]
     meta = collections.OrderedDict(
         method="RHF", basis=opt["basis"], n_basis=mol["K"], system=_system_string([s for s, _ in opt["config"]]),
@@ -257,7 +259,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m hartree_fock_cpp_gb300.apps")
     ap.add_argument("app", choices=["single_run", "bl_scan", "dissociation"])
     ap.add_argument("input")
-    ap.add_argument("--batched", action="store_true", help="bl_scan: all points concurrently on the server")
+    ap.add_argument("--batched", action="store_true", help="bl_scan: all points at once on one packed job")
     a = ap.parse_args(argv)
     if a.app == "single_run":
         r = run_scf_from_options(read_scf_options(a.input))

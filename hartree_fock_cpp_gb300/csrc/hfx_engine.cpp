@@ -132,6 +132,7 @@ Job::Job(const std::vector<Basis>& mols, const hfx_options& opt) : opt_(opt)
 {
     if (mols.empty() || mols.size() > 65535) throw Error(HFX_ERR_INVALID, "packed job: 1..65535 molecules");
     basis_ = concat_basis(mols, frags_);
+    packed_ = true;
     init(opt);
 }
 
@@ -236,7 +237,7 @@ void Job::init(const hfx_options& opt)
         }
         d_fk_.upload(fk, stream_);
         d_fmoff_.upload(fm, stream_);
-        if (F > 1) {
+        if (packed_) {
             std::vector<unsigned char> on(F, 1);
             d_active_.upload(on, stream_);
         }

@@ -295,6 +295,7 @@ private:
     DevBuf<int> d_fk_;              // per molecule K_f
     DevBuf<long long> d_fmoff_;     // per molecule matrix offset
     DevBuf<unsigned char> d_active_;   // packed jobs: per molecule build flag
+    bool packed_ = false;              // built by the packed (several-molecule) constructor
 
     std::vector<HostPair> hpairs_;
     GroupSet gs_fp64_, gs_mixed_;
