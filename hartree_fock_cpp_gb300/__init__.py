@@ -312,14 +312,18 @@ def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsil
     return out, stats
 
 
-def one_electron(config, basis_set, param_path=None):
-    """(S, T, V) of the molecule (integrals.hpp:10-536), host."""
+def one_electron(config, basis_set, param_path=None, gpu=False, device=0):
+    """(S, T, V) of the molecule (integrals.hpp:10-536), on the host or, with
+    gpu=True, on CUDA device `device`."""
     m = _lib.MoleculeArgs(config, basis_set, param_path)
     K = ctypes.c_int()
     check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
     K = K.value
     S, T, Vm = np.zeros((K, K)), np.zeros((K, K)), np.zeros((K, K))
-    check(lib.hfx_one_electron(m.ref(), ptr(S), ptr(T), ptr(Vm), None))
+    if gpu:
+        check(lib.hfx_one_electron_gpu(m.ref(), int(device), ptr(S), ptr(T), ptr(Vm), None))
+    else:
+        check(lib.hfx_one_electron(m.ref(), ptr(S), ptr(T), ptr(Vm), None))
     return S, T, Vm
 
 

@@ -135,6 +135,10 @@ SIGNATURES = {
     "hfx_build_functions": (I, [V, P(I), P(I), V, V, V, V, V, V]),
     "hfx_debug_pair_data": (I, [V, P(I), P(I), P(ctypes.c_longlong), V, V, V]),
     "hfx_one_electron": (I, [V, V, V, V, P(I)]),
+    "hfx_one_electron_gpu": (I, [V, I, V, V, V, P(I)]),
+    "hfx_grid_density": (I, [V, I, V, V, D, I, V]),
+    "hfx_grid_orbital": (I, [V, I, V, I, V, D, I, V]),
+    "hfx_points_eval": (I, [V, I, V, I, V, ctypes.c_longlong, V]),
     "hfx_last_error": (I, [ctypes.c_char_p, ctypes.c_size_t]),
     "hfx_measure_peaks": (I, [I, P(D), P(D)]),
     "hfx_server_create": (I, [V, P(V)]),

@@ -27,6 +27,8 @@ namespace hfx {
 // in the mixed-precision SCF (Q_AB Q_CD max|dD| below this: quartet skipped)
 constexpr double kDeltaThr = 1e-12;
 void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG);   // hfx_noalloc.cu
+void grid_eval(const Basis& b, int device, const double* M, int column, const double* xyz, long long n, int res,
+               const double* start, const double* step, double* out);                  // hfx_grid.cu
 static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace hfx
@@ -275,6 +277,21 @@ hfx_status hfx_last_build_stats(const hfx_job* job, hfx_build_stats* stats)
     });
 }
 
+// The reference's box_points (cube.hpp:137-168): linspace(c - L/2, c + L/2, res) per axis.
+static void box_eval(const Basis& b, int device, const double* M, int column, const double* center, double L, int res,
+                     double* out)
+{
+    if (res < 2) throw Error(HFX_ERR_INVALID, "resolution must be at least 2");
+    if (res > 2048) throw Error(HFX_ERR_INVALID, "resolution above 2048");
+    double start[3], step[3];
+    for (int d = 0; d < 3; ++d) {
+        const double lo = center[d] - L / 2, hi = center[d] + L / 2;
+        start[d] = lo;
+        step[d] = (hi - lo) / (res - 1);
+    }
+    grid_eval(b, device, M, column, nullptr, (long long)res * res * res, res, start, step, out);
+}
+
 static void fill_result(const ScfOutput& o, hfx_scf_result* r, double fock_ms)
 {
     if (!r) return;
@@ -314,7 +331,7 @@ hfx_status hfx_rhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, con
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
-        ScfSetup setup = scf_setup(b);
+        ScfSetup setup = scf_setup(b, true);
         DeviceScf d(job, setup, 1);
         ScfOutput out = d.run(b, setup, o, 0, 0, P0, nullptr, kDeltaThr);
         fill_result(out, res, out.fock_ms);
@@ -337,7 +354,7 @@ hfx_status hfx_uhf_diis(const hfx_molecule* mol, const hfx_scf_options* opt, int
         if (opt) o = *opt;
         Basis b = build_basis(*mol);
         Job job(b, job_options(&o));
-        ScfSetup setup = scf_setup(b);
+        ScfSetup setup = scf_setup(b, true);
         DeviceScf d(job, setup, 2);
         ScfOutput out = d.run(b, setup, o, n_alpha, n_beta, Pa0, Pb0, kDeltaThr);
         fill_result(out, res, out.fock_ms);
@@ -354,7 +371,7 @@ static const ScfSetup& job_setup(hfx_job* job)
 {
     if (job->job->basis().atom_Z.empty())
         throw Error(HFX_ERR_INVALID, "SCF needs a job created from a molecule (nuclear charges)");
-    if (!job->setup) job->setup = std::make_unique<ScfSetup>(scf_setup(job->job->basis()));
+    if (!job->setup) job->setup = std::make_unique<ScfSetup>(scf_setup(job->job->basis(), true));
     return *job->setup;
 }
 
@@ -445,6 +462,66 @@ hfx_status hfx_one_electron(const hfx_molecule* mol, double* S, double* T, doubl
         if (!S && !T && !V) return;
         std::vector<double> s, t, v;
         one_electron(b, s, t, v);
+        if (S) std::memcpy(S, s.data(), s.size() * sizeof(double));
+        if (T) std::memcpy(T, t.data(), t.size() * sizeof(double));
+        if (V) std::memcpy(V, v.data(), v.size() * sizeof(double));
+    });
+}
+
+static void check_device(int device)
+{
+    int ndev = 0;
+    cuda_check(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+    if (device < 0 || device >= ndev) throw Error(HFX_ERR_INVALID, "invalid CUDA device ordinal");
+}
+
+hfx_status hfx_grid_density(const hfx_functions* basis, int device, const double* P, const double* center, double L,
+                            int res, double* rho)
+{
+    return guarded([&] {
+        if (!basis || !P || !center || !rho) throw Error(HFX_ERR_INVALID, "null argument");
+        check_device(device);
+        box_eval(basis_from_functions(*basis), device, P, -1, center, L, res, rho);
+    });
+}
+
+hfx_status hfx_grid_orbital(const hfx_functions* basis, int device, const double* C, int column, const double* center,
+                            double L, int res, double* psi)
+{
+    return guarded([&] {
+        if (!basis || !C || !center || !psi) throw Error(HFX_ERR_INVALID, "null argument");
+        if (column < 0 || column >= basis->K) throw Error(HFX_ERR_INVALID, "orbital index out of range");
+        check_device(device);
+        box_eval(basis_from_functions(*basis), device, C, column, center, L, res, psi);
+    });
+}
+
+hfx_status hfx_points_eval(const hfx_functions* basis, int device, const double* M, int column, const double* xyz,
+                           long long n, double* out)
+{
+    return guarded([&] {
+        if (!basis || !M || (n > 0 && (!xyz || !out))) throw Error(HFX_ERR_INVALID, "null argument");
+        if (n < 0) throw Error(HFX_ERR_INVALID, "negative point count");
+        if (column >= basis->K) throw Error(HFX_ERR_INVALID, "orbital index out of range");
+        check_device(device);
+        if (n == 0) return;
+        grid_eval(basis_from_functions(*basis), device, M, column < 0 ? -1 : column, xyz, n, 0, nullptr, nullptr, out);
+    });
+}
+
+hfx_status hfx_one_electron_gpu(const hfx_molecule* mol, int device, double* S, double* T, double* V, int* K)
+{
+    return guarded([&] {
+        if (!mol) throw Error(HFX_ERR_INVALID, "null molecule");
+        int ndev = 0;
+        cuda_check(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+        if (device < 0 || device >= ndev) throw Error(HFX_ERR_INVALID, "invalid CUDA device ordinal");
+        cuda_check(cudaSetDevice(device), "cudaSetDevice");
+        Basis b = build_basis(*mol);
+        if (K) *K = b.K;
+        if (!S && !T && !V) return;
+        std::vector<double> s, t, v;
+        one_electron_gpu(b, s, t, v);
         if (S) std::memcpy(S, s.data(), s.size() * sizeof(double));
         if (T) std::memcpy(T, t.data(), t.size() * sizeof(double));
         if (V) std::memcpy(V, v.data(), v.size() * sizeof(double));

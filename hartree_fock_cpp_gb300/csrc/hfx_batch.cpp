@@ -269,7 +269,7 @@ extern "C" hfx_status hfx_batch_scf(const hfx_molecule* mols, int n, const int* 
             for (int i = next++; i < n; i = next++) {
                 bool joined = false;
                 try {
-                    ScfSetup setup = scf_setup(bases[i]);
+                    ScfSetup setup = scf_setup(bases[i], true);
                     BatchMember member(builder, i, bases[i].K, job.mixed());
                     DeviceScf d(member, setup, nspin);
                     builder.join();

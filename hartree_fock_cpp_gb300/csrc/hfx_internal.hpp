@@ -65,6 +65,8 @@ int element_Z(const std::string& sym);
 
 // Host one-electron matrices (K x K row-major).
 void one_electron(const Basis& b, std::vector<double>& S, std::vector<double>& T, std::vector<double>& V);
+// The same matrices computed on the current CUDA device (hfx_onee_gpu.cu).
+void one_electron_gpu(const Basis& b, std::vector<double>& S, std::vector<double>& T, std::vector<double>& V);
 
 // 1-D Hermite expansion coefficients E^{ij}_t (integrals.hpp:269-322
 // recursion) for i <= imax, j <= jmax, stored

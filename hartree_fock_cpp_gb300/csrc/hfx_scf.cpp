@@ -138,13 +138,16 @@ static bool finite_all(const std::vector<double>& v)
     return true;
 }
 
-ScfSetup scf_setup(const Basis& b)
+ScfSetup scf_setup(const Basis& b, bool gpu)
 {
     ScfSetup s;
     int K = b.K;
     s.K = K;
     std::vector<double> T, V;
-    one_electron(b, s.S, T, V);
+    if (gpu)
+        one_electron_gpu(b, s.S, T, V);
+    else
+        one_electron(b, s.S, T, V);
     s.H.resize((size_t)K * K);
     for (int i = 0; i < K * K; ++i) s.H[i] = T[i] + V[i];
     s.E_nuc = nuclear_repulsion(b);

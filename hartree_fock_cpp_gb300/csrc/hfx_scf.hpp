@@ -38,7 +38,8 @@ struct ScfSetup {
     std::vector<double> S, H, X;
     double E_nuc = 0.0;
 };
-ScfSetup scf_setup(const Basis& b);
+// gpu: S, T, V on the current CUDA device instead of the host
+ScfSetup scf_setup(const Basis& b, bool gpu = false);
 
 ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options& opt, const double* P0,
                    const GBuilder& g);

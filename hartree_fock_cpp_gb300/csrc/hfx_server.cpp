@@ -294,7 +294,7 @@ private:
             o.fp32_threshold = j->fp32_threshold;
             o.device = opt_.device;
             Job job(b, o);
-            ScfSetup setup = scf_setup(b);
+            ScfSetup setup = scf_setup(b, true);
             DeviceScf d(job, setup, j->method == 1 ? 2 : 1);
             const double deadline = j->timeout_s > 0 ? j->t_submit + j->timeout_s : 0.0;
             ScfControl ctl{&j->cancel, deadline, j->inject_fault == HFX_FAULT_ITERATION ? 3 : 0};

@@ -253,6 +253,9 @@ hfx_status hfx_debug_pair_data(const hfx_molecule *mol, int *npairs, int *nprimp
 
 /* One-electron matrices S, T, V of a molecule (integrals.hpp:10-536), host. */
 hfx_status hfx_one_electron(const hfx_molecule *mol, double *S, double *T, double *V, int *K);
+/* The same matrices computed on CUDA device `device` (one CTA per shell pair;
+ * the SCF entry points use this for their setup).  Host output buffers. */
+hfx_status hfx_one_electron_gpu(const hfx_molecule *mol, int device, double *S, double *T, double *V, int *K);
 
 /* ---- request server (continuous batching on one GPU) ---------------------- */
 
@@ -346,6 +349,25 @@ typedef struct {
 hfx_status hfx_batch_scf(const hfx_molecule *mols, int n, const int *n_alpha, const int *n_beta,
                          const hfx_scf_options *scf, const hfx_batch_options *opt, hfx_scf_result *results,
                          hfx_batch_stats *stats);
+
+/* ---- electron density and orbitals on grids (cube.hpp:9-168, evaluation.cuh:59-123) ----
+ * rho(r) = sum_{mu,nu} P_{mu nu} phi_mu(r) phi_nu(r), psi_i(r) = sum_mu C_{mu i} phi_mu(r)
+ * with the basis functions of `basis` (the reference's std::vector<basis_function>,
+ * as density_gpu / orbital_gpu take it, visual.cu), on CUDA device `device`.
+ * Box grids follow density3d / homo_lumo_3d:
+ * res^3 points x_i = (c - L/2) + i (L / (res - 1)) per axis, value of point
+ * (i, j, k) at out[(i * res + j) * res + k]; res >= 2.  P and C are K x K
+ * row-major host matrices (C's column `column` is the orbital); out is host
+ * memory.  Limits: K such that a 32-point tile of all functions fits in
+ * shared memory (K <= ~880), at most 32 primitives per shell. */
+hfx_status hfx_grid_density(const hfx_functions *basis, int device, const double *P, const double *center, double L,
+                            int res, double *rho);
+hfx_status hfx_grid_orbital(const hfx_functions *basis, int device, const double *C, int column, const double *center,
+                            double L, int res, double *psi);
+/* The same at n explicit points (xyz: 3n, bohr): column < 0 evaluates rho
+ * with M = P, column >= 0 evaluates psi_column with M = C. */
+hfx_status hfx_points_eval(const hfx_functions *basis, int device, const double *M, int column, const double *xyz,
+                           long long n, double *out);
 
 /* Last error message of the calling thread (empty if none). */
 hfx_status hfx_last_error(char *buf, size_t n);

@@ -223,6 +223,53 @@ class Oracle:
         return S, T, V
 
 
+# ---------------- grid evaluation (cube.hpp:9-168) ----------------
+
+def linspace(start, stop, n):               # visual.hpp:42-51
+    step = (stop - start) / (n - 1)
+    return [start + i * step for i in range(n)]
+
+
+def box_points(center, L, res):             # cube.hpp:137-168, index3d order (indexing.hpp:10-12)
+    x = linspace(center[0] - L / 2, center[0] + L / 2, res)
+    y = linspace(center[1] - L / 2, center[1] + L / 2, res)
+    z = linspace(center[2] - L / 2, center[2] + L / 2, res)
+    X, Y, Z = np.meshgrid(np.array(x), np.array(y), np.array(z), indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+
+
+def basis_values(fb, r):
+    """phi_mu(r) for every basis function and point, function_eval
+    (cube.hpp:9-41): sum_i N_i c_i (x-Ax)^l (y-Ay)^m (z-Az)^n exp(-a_i d^2)."""
+    r = np.asarray(r, dtype=np.float64).reshape(-1, 3)
+    phi = np.zeros((fb.K, r.shape[0]))
+    lmn = fb.lmn.reshape(-1, 3)
+    for mu in range(fb.K):
+        A = fb.centres[mu]
+        dx, dy, dz = r[:, 0] - A[0], r[:, 1] - A[1], r[:, 2] - A[2]
+        d2 = dx * dx + dy * dy + dz * dz
+        l, m, n = (int(v) for v in lmn[mu])
+        val = np.zeros(r.shape[0])
+        for i in range(fb.prim_off[mu], fb.prim_off[mu + 1]):
+            val += fb.norm[i] * fb.coeff[i] * dx ** l * dy ** m * dz ** n * np.exp(-fb.alpha[i] * d2)
+        phi[mu] = val
+    return phi
+
+
+def electron_density(fb, P, r):             # cube.hpp:44-93: sum over pairs, 2x off-diagonal
+    phi = basis_values(fb, r)
+    P = np.asarray(P).reshape(fb.K, fb.K)
+    iu = np.triu_indices(fb.K)
+    w = np.where(iu[0] == iu[1], 1.0, 2.0) * P[iu]
+    return np.einsum("p,pn,pn->n", w, phi[iu[0]], phi[iu[1]])
+
+
+def orbital_wf(fb, C, idx, r):              # cube.hpp:96-135
+    phi = basis_values(fb, r)
+    C = np.asarray(C).reshape(fb.K, fb.K)
+    return C[:, idx] @ phi
+
+
 def repulsion_matrix(P, eri):               # linalg.hpp:100-129
     K = P.shape[0]
     P = np.ascontiguousarray(P, dtype=np.float64)

@@ -207,3 +207,18 @@ def test_graph_replayed_builds_match_first_eager_build(precision):
     for a, b in zip(Us, Ue):
         for x, y in zip(a, b):
             assert np.abs(x - y).max() < 1e-11
+
+
+# ---------------- one-electron matrices on the device ----------------
+
+@pytest.mark.parametrize("cfg,basis", [(W.water(), "STO-3G"), (W.water(), "cc-pVTZ"), (W.benzene(), "cc-pVDZ"),
+                                       (W.nacl_scan(8)[3], "cc-pVTZ")])
+def test_one_electron_gpu_matches_host_and_oracle(cfg, basis):
+    S0, T0, V0 = H.one_electron(cfg, basis)
+    S1, T1, V1 = H.one_electron(cfg, basis, gpu=True)
+    for a, b in ((S0, S1), (T0, T1), (V0, V1)):
+        assert np.abs(a - b).max() < 1e-10
+    if basis == "STO-3G":
+        g = _gold("water_sto3g.json")
+        for key, M in (("S", S1), ("T", T1), ("V", V1)):
+            assert np.abs(np.array(g[key]).reshape(M.shape) - M).max() < 1e-10
