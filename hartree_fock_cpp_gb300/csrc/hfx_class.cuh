@@ -274,35 +274,136 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     double* Kx = a.Kx + bra.moff;
     double* Kx2 = a.Kx2 + (NK == 2 ? bra.moff : 0);
     const bool same_pair = (tk.bra == tk.ket);
+    if constexpr (sizeof(T) == 8) {
 #pragma unroll
-    for (int ab = 0; ab < NAB; ++ab) {
-        const int ia = ab / NB, ib = ab % NB;
-        const int i = bra.bf0 + ia, j = bra.bf1 + ib;
-        const long long pij = spidx(i, j);
-        const double qb = __ldg(Qbf + pij);
-        if (bra.same && ia < ib) continue;
+        for (int ab = 0; ab < NAB; ++ab) {
+            const int ia = ab / NB, ib = ab % NB;
+            const int i = bra.bf0 + ia, j = bra.bf1 + ib;
+            const long long pij = spidx(i, j);
+            const double qb = __ldg(Qbf + pij);
+            if (bra.same && ia < ib) continue;
+#pragma unroll
+            for (int cd = 0; cd < NCD; ++cd) {
+                const int ic = cd / ND, id = cd % ND;
+                const int k = ket.bf0 + ic, l = ket.bf1 + id;
+                if (ket.same && ic < id) continue;
+                const long long pkl = spidx(k, l);
+                if (same_pair && pij < pkl) continue;
+                if (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr) continue;
+                const double v =
+                    (double)acc[ab][cd] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
+                atomicAdd(J + (long long)i * K + j, __ldg(Dj + (long long)k * K + l) * v);
+                atomicAdd(J + (long long)k * K + l, __ldg(Dj + (long long)i * K + j) * v);
+                atomicAdd(Kx + (long long)i * K + k, __ldg(Dk + (long long)j * K + l) * v);
+                atomicAdd(Kx + (long long)j * K + l, __ldg(Dk + (long long)i * K + k) * v);
+                atomicAdd(Kx + (long long)i * K + l, __ldg(Dk + (long long)j * K + k) * v);
+                atomicAdd(Kx + (long long)j * K + k, __ldg(Dk + (long long)i * K + l) * v);
+                if constexpr (NK == 2) {
+                    atomicAdd(Kx2 + (long long)i * K + k, __ldg(Dk2 + (long long)j * K + l) * v);
+                    atomicAdd(Kx2 + (long long)j * K + l, __ldg(Dk2 + (long long)i * K + k) * v);
+                    atomicAdd(Kx2 + (long long)i * K + l, __ldg(Dk2 + (long long)j * K + k) * v);
+                    atomicAdd(Kx2 + (long long)j * K + k, __ldg(Dk2 + (long long)i * K + l) * v);
+                }
+            }
+        }
+    } else {
+        // FP32 quartets: the degeneracy weight is applied in place (0 for the
+        // non-canonical and BF-screened elements); then every J / K element
+        // the quartet touches is summed over the quartet in registers (float
+        // products with the float density copies) and added to the FP64
+        // accumulators once -- nab + ncd + na nc + na nd + nb nc + nb nd
+        // atomics per quartet instead of 6 per integral.
+        constexpr int NA = c_nc(LA), NC = c_nc(LC);
+#pragma unroll
+        for (int ab = 0; ab < NAB; ++ab) {
+            const int ia = ab / NB, ib = ab % NB;
+            const int i = bra.bf0 + ia, j = bra.bf1 + ib;
+            const long long pij = spidx(i, j);
+            const double qb = __ldg(Qbf + pij);
+#pragma unroll
+            for (int cd = 0; cd < NCD; ++cd) {
+                const int ic = cd / ND, id = cd % ND;
+                const int k = ket.bf0 + ic, l = ket.bf1 + id;
+                const long long pkl = spidx(k, l);
+                const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) || (same_pair && pij < pkl) ||
+                                  (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr);
+                const float f = (i == j ? 1.f : 2.f) * (k == l ? 1.f : 2.f) * (pij == pkl ? 1.f : 2.f);
+                acc[ab][cd] = skip ? 0.f : acc[ab][cd] * f;
+            }
+        }
+        const float* __restrict__ Dj32 = a.Dj32 + bra.moff;
+        const int i0 = bra.bf0, j0 = bra.bf1, k0 = ket.bf0, l0 = ket.bf1;
+        auto d32 = [&](const float* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
+        auto put = [&](double* M, int r, int c, float v) {
+            if (v != 0.f) atomicAdd(M + (long long)r * K + c, (double)v);
+        };
+#pragma unroll
+        for (int ab = 0; ab < NAB; ++ab) {
+            float sj = 0.f;
+#pragma unroll
+            for (int cd = 0; cd < NCD; ++cd) sj += d32(Dj32, k0 + cd / ND, l0 + cd % ND) * acc[ab][cd];
+            put(J, i0 + ab / NB, j0 + ab % NB, sj);
+        }
 #pragma unroll
         for (int cd = 0; cd < NCD; ++cd) {
-            const int ic = cd / ND, id = cd % ND;
-            const int k = ket.bf0 + ic, l = ket.bf1 + id;
-            if (ket.same && ic < id) continue;
-            const long long pkl = spidx(k, l);
-            if (same_pair && pij < pkl) continue;
-            if (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr) continue;
-            const double v =
-                (double)acc[ab][cd] * ((i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0));
-            atomicAdd(J + (long long)i * K + j, __ldg(Dj + (long long)k * K + l) * v);
-            atomicAdd(J + (long long)k * K + l, __ldg(Dj + (long long)i * K + j) * v);
-            atomicAdd(Kx + (long long)i * K + k, __ldg(Dk + (long long)j * K + l) * v);
-            atomicAdd(Kx + (long long)j * K + l, __ldg(Dk + (long long)i * K + k) * v);
-            atomicAdd(Kx + (long long)i * K + l, __ldg(Dk + (long long)j * K + k) * v);
-            atomicAdd(Kx + (long long)j * K + k, __ldg(Dk + (long long)i * K + l) * v);
-            if constexpr (NK == 2) {
-                atomicAdd(Kx2 + (long long)i * K + k, __ldg(Dk2 + (long long)j * K + l) * v);
-                atomicAdd(Kx2 + (long long)j * K + l, __ldg(Dk2 + (long long)i * K + k) * v);
-                atomicAdd(Kx2 + (long long)i * K + l, __ldg(Dk2 + (long long)j * K + k) * v);
-                atomicAdd(Kx2 + (long long)j * K + k, __ldg(Dk2 + (long long)i * K + l) * v);
-            }
+            float sj = 0.f;
+#pragma unroll
+            for (int ab = 0; ab < NAB; ++ab) sj += d32(Dj32, i0 + ab / NB, j0 + ab % NB) * acc[ab][cd];
+            put(J, k0 + cd / ND, l0 + cd % ND, sj);
+        }
+#pragma unroll
+        for (int sp = 0; sp < NK; ++sp) {
+            const float* __restrict__ Dk32 = (sp == 0 ? a.Dk32 : a.Dk232) + bra.moff;
+            double* KK = sp == 0 ? Kx : Kx2;
+            // K_ik += D_jl v, K_jl += D_ik v, K_il += D_jk v, K_jk += D_il v
+#pragma unroll
+            for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                for (int ic = 0; ic < NC; ++ic) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                        for (int id = 0; id < ND; ++id)
+                            s += d32(Dk32, j0 + ib, l0 + id) * acc[ia * NB + ib][ic * ND + id];
+                    put(KK, i0 + ia, k0 + ic, s);
+                }
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                for (int id = 0; id < ND; ++id) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                        for (int ic = 0; ic < NC; ++ic)
+                            s += d32(Dk32, i0 + ia, k0 + ic) * acc[ia * NB + ib][ic * ND + id];
+                    put(KK, j0 + ib, l0 + id, s);
+                }
+#pragma unroll
+            for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                for (int id = 0; id < ND; ++id) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                        for (int ic = 0; ic < NC; ++ic)
+                            s += d32(Dk32, j0 + ib, k0 + ic) * acc[ia * NB + ib][ic * ND + id];
+                    put(KK, i0 + ia, l0 + id, s);
+                }
+#pragma unroll
+            for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+                for (int ic = 0; ic < NC; ++ic) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+                        for (int id = 0; id < ND; ++id)
+                            s += d32(Dk32, i0 + ia, l0 + id) * acc[ia * NB + ib][ic * ND + id];
+                    put(KK, j0 + ib, k0 + ic, s);
+                }
         }
     }
 }

@@ -167,6 +167,10 @@ struct SmallArgs {
     const double* Dsh;         // per shell pair max |D| (density screening), or null
     double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
     const unsigned char* active;   // packed jobs: per molecule, 0 = skip its quartets (null: all)
+    // FP32 kernels: float copies of Dj / Dk / Dk2 for the block digestion
+    const float* Dj32;
+    const float* Dk32;
+    const float* Dk232;
 };
 
 // Arguments of the warp-per-shell-quartet kernel.
@@ -198,6 +202,10 @@ struct WarpArgs {
     double* Qout_bf;           // Schwarz pass (NK = 0): BF-pair bounds out
     unsigned long long* Qout_sh;   // Schwarz pass: per shell pair max bound (double bits)
     const unsigned char* active;   // packed jobs: per molecule, 0 = skip its quartets (null: all)
+    // FP32 kernels: float copies of Dj / Dk / Dk2 for the block digestion
+    const float* Dj32;
+    const float* Dk32;
+    const float* Dk232;
 };
 
 #ifdef __CUDACC__

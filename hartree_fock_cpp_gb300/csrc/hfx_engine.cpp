@@ -263,11 +263,16 @@ Job::~Job()
     if (stream_) cudaStreamDestroy(stream_);
 }
 
-bool is_small_class(int pcb, int pck)
+bool is_small_class(int pcb, int pck, bool fp32)
 {
     static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0}};
+    // FP32 only: thread-per-quartet forms that fit the register file in float
+    static const int small32[][2] = {{2, 2}, {3, 2}, {4, 1}, {4, 3}};
     for (auto& c : small)
         if (c[0] == pcb && c[1] == pck) return true;
+    if (fp32)
+        for (auto& c : small32)
+            if (c[0] == pcb && c[1] == pck) return true;
     return false;
 }
 
@@ -608,7 +613,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             const HostPair& k = hpairs_[ket];
             const double fpp = flops_per_prim(b.l0, b.l1, k.l0, k.l1);
             const int pcb = pcof(bra), pck = pcof(ket);
-            const bool sm = is_small_class(pcb, pck);
+            const bool sm = is_small_class(pcb, pck, f32);
             Bucket& bk = sm ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
             // split the bra primitive pairs so that a chunk holds at most
             // kChunkPrims primitive quartets (per thread) or 16x that (per warp)
@@ -815,10 +820,40 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
         sk.kernel(0, density_blocks_spec(np), prm);
         Dsh = d_dsh_.p;
     }
+    // float copies of the densities for the FP32 groups' block digestion
+    const float *Dj32 = nullptr, *Dk32 = nullptr, *Dk232 = nullptr;
+    bool any32 = false;
+    for (const auto& g : groups) any32 = any32 || (g.fp32 && g.n > 0);
+    if (any32) {
+        long long n = nmat();
+        d_d32_.alloc((size_t)3 * n);
+        const double* src[3] = {Dj, Dk, Dk2};
+        const float* dst[3] = {nullptr, nullptr, nullptr};
+        for (int s = 0; s < 3; ++s) {
+            if (!src[s]) continue;
+            int same = -1;
+            for (int q = 0; q < s; ++q)
+                if (src[q] == src[s]) same = q;
+            if (same >= 0) {
+                dst[s] = dst[same];
+                continue;
+            }
+            const double* in = src[s];
+            float* out = d_d32_.p + (size_t)s * n;
+            void* prm[] = {&in, &out, &n};
+            sk.kernel(0, to_float_spec(n), prm);
+            dst[s] = out;
+        }
+        Dj32 = dst[0];
+        Dk32 = dst[1];
+        Dk232 = dst[2];
+    }
     int* ctr = counters ? counters : d_counters_.p;
     sk.zero(0, ctr, sizeof(int) * std::max<size_t>(1, groups.size()));
     sk.fork();
-    // warp groups (the long ones) on the main lane, small classes spread over the others
+    // warp groups (the long ones) on the main lane, small classes spread over
+    // the others (running the FP32 warp groups on a lane of their own, beside
+    // the FP64 ones, measured slower: the persistent grids contend for SMs)
     const int naux = (int)aux_.size();
     int next_aux = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
@@ -830,7 +865,8 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
             next_aux = (next_aux + 1) % naux;
             if (g.fp32) {
                 SmallArgs<float> a{d_pairs_.p, d_rec32_.p, tasks + g.off, (int)g.n, d_boys32_.p,
-                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active};
+                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active,
+                                   Dj32, Dk32, Dk232};
                 cuda_check(small_spec_f32(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
@@ -848,7 +884,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                   tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
-                                  Dsh, dthr, nullptr, nullptr, active};
+                                  Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             } else {

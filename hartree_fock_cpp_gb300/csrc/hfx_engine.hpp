@@ -22,13 +22,14 @@ cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, in
 KernelSpec finish_rhf_spec(int Kmax, int nfrag);   // k_finish_rhf(Jacc, Kacc, G, fk, fmoff, active)
 KernelSpec finish_uhf_spec(int Kmax, int nfrag);   // k_finish_uhf(Jacc, Ka, Kb, J, Kao, Kbo, fk, fmoff, active)
 KernelSpec add_spec(long long n);    // k_add(A, B, C, n)
+KernelSpec to_float_spec(long long n);   // k_to_float(A, B, n)
 KernelSpec density_blocks_spec(int npairs);   // k_density_blocks(pairs, npairs, D1, D2, Dsh)
 cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<double>)
 cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<float>)
 cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s);
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
 int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
-bool is_small_class(int pcb, int pck);
+bool is_small_class(int pcb, int pck, bool fp32);
 
 void cuda_check(cudaError_t e, const char* what);
 
@@ -301,6 +302,7 @@ private:
     GroupSet gs_fp64_, gs_mixed_;
     DevBuf<int> d_counters_;
     DevBuf<double> d_dsh_;
+    DevBuf<float> d_d32_;           // float copies of the build's densities (FP32 groups)
     std::vector<DPair> dpairs_host_;
     DevBuf<double> d_rec64_;
     DevBuf<float> d_rec32_;

@@ -290,6 +290,13 @@ __global__ void k_finish_uhf(const double* Jacc, const double* Ka, const double*
     }
 }
 
+// float copy of a packed density (the FP32 kernels' digestion products)
+__global__ void k_to_float(const double* A, float* B, long long n)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        B[e] = (float)A[e];
+}
+
 __global__ void k_add(const double* A, const double* B, double* C, long long n)
 {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
@@ -385,5 +392,6 @@ KernelSpec finish_uhf_spec(int Kmax, int nfrag)
     return elementwise_spec((const void*)k_finish_uhf, (long long)Kmax * Kmax, nfrag);
 }
 KernelSpec add_spec(long long n) { return elementwise_spec((const void*)k_add, n, 1); }
+KernelSpec to_float_spec(long long n) { return elementwise_spec((const void*)k_to_float, n, 1); }
 
 }  // namespace hfx

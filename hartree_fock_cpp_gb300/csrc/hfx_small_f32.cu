@@ -5,6 +5,8 @@ namespace hfx {
 
 // Pair class index pc = l0*(l0+1)/2 + l1; bra pc >= ket pc.  Returns
 // cudaErrorInvalidValue for a class that has no small-class kernel.
+cudaError_t small_spec_f32x(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // hfx_small_f32x.cu
+
 cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
 {
     switch (pcb * 16 + pck) {
@@ -17,7 +19,7 @@ cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
     case 3 * 16 + 1: return small_spec<float, 2, 0, 1, 0>(nk, ntasks, s);   // (ds|ps)
     case 3 * 16 + 3: return small_spec<float, 2, 0, 2, 0>(nk, ntasks, s);   // (ds|ds)
     case 4 * 16 + 0: return small_spec<float, 2, 1, 0, 0>(nk, ntasks, s);   // (dp|ss)
-    default: return cudaErrorInvalidValue;
+    default: return small_spec_f32x(pcb, pck, nk, ntasks, s);
     }
 }
 
