@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     double* Kx = a.Kx + bra.moff;
     double* Kx2 = a.Kx2 + (NK == 2 ? bra.moff : 0);
     const bool same_pair = (tk.bra == tk.ket);
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (sizeof(T) == 8 && !kBlockDigestFP64) {
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) {
             const int ia = ab / NB, ib = ab % NB;
@@ -307,12 +307,12 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             }
         }
     } else {
-        // FP32 quartets: the degeneracy weight is applied in place (0 for the
-        // non-canonical and BF-screened elements); then every J / K element
-        // the quartet touches is summed over the quartet in registers (float
-        // products with the float density copies) and added to the FP64
-        // accumulators once -- nab + ncd + na nc + na nd + nb nc + nb nd
-        // atomics per quartet instead of 6 per integral.
+        // Block digestion: the degeneracy weight is applied in place (0 for
+        // the non-canonical and BF-screened elements); then every J / K
+        // element the quartet touches is summed over the quartet in registers
+        // (FP32 quartets: float products with the float density copies) and
+        // added to the FP64 accumulators once -- nab + ncd + na nc + na nd +
+        // nb nc + nb nd atomics per quartet instead of 6 per integral.
         constexpr int NA = c_nc(LA), NC = c_nc(LC);
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) {
@@ -327,40 +327,41 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
                 const long long pkl = spidx(k, l);
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) || (same_pair && pij < pkl) ||
                                   (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr);
-                const float f = (i == j ? 1.f : 2.f) * (k == l ? 1.f : 2.f) * (pij == pkl ? 1.f : 2.f);
-                acc[ab][cd] = skip ? 0.f : acc[ab][cd] * f;
+                const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
+                acc[ab][cd] = skip ? (T)0 : acc[ab][cd] * f;
             }
         }
-        const float* __restrict__ Dj32 = a.Dj32 + bra.moff;
+        const T* __restrict__ Dj32 = density_of<T>(a.Dj, a.Dj32) + bra.moff;
         const int i0 = bra.bf0, j0 = bra.bf1, k0 = ket.bf0, l0 = ket.bf1;
-        auto d32 = [&](const float* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
-        auto put = [&](double* M, int r, int c, float v) {
-            if (v != 0.f) atomicAdd(M + (long long)r * K + c, (double)v);
+        auto d32 = [&](const T* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
+        auto put = [&](double* M, int r, int c, T v) {
+            if (v != (T)0) atomicAdd(M + (long long)r * K + c, (double)v);
         };
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) {
-            float sj = 0.f;
+            T sj = 0;
 #pragma unroll
             for (int cd = 0; cd < NCD; ++cd) sj += d32(Dj32, k0 + cd / ND, l0 + cd % ND) * acc[ab][cd];
             put(J, i0 + ab / NB, j0 + ab % NB, sj);
         }
 #pragma unroll
         for (int cd = 0; cd < NCD; ++cd) {
-            float sj = 0.f;
+            T sj = 0;
 #pragma unroll
             for (int ab = 0; ab < NAB; ++ab) sj += d32(Dj32, i0 + ab / NB, j0 + ab % NB) * acc[ab][cd];
             put(J, k0 + cd / ND, l0 + cd % ND, sj);
         }
 #pragma unroll
         for (int sp = 0; sp < NK; ++sp) {
-            const float* __restrict__ Dk32 = (sp == 0 ? a.Dk32 : a.Dk232) + bra.moff;
+            const T* __restrict__ Dk32 =
+                (sp == 0 ? density_of<T>(a.Dk, a.Dk32) : density_of<T>(a.Dk2, a.Dk232)) + bra.moff;
             double* KK = sp == 0 ? Kx : Kx2;
             // K_ik += D_jl v, K_jl += D_ik v, K_il += D_jk v, K_jk += D_il v
 #pragma unroll
             for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                 for (int ic = 0; ic < NC; ++ic) {
-                    float s = 0.f;
+                    T s = 0;
 #pragma unroll
                     for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
@@ -372,7 +373,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                 for (int id = 0; id < ND; ++id) {
-                    float s = 0.f;
+                    T s = 0;
 #pragma unroll
                     for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                 for (int id = 0; id < ND; ++id) {
-                    float s = 0.f;
+                    T s = 0;
 #pragma unroll
                     for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                 for (int ic = 0; ic < NC; ++ic) {
-                    float s = 0.f;
+                    T s = 0;
 #pragma unroll
                     for (int ia = 0; ia < NA; ++ia)
 #pragma unroll

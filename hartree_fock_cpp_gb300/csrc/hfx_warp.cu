@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         double* J = a.J + bra.moff;
         double* Kx = a.Kx + bra.moff;
         double* Kx2 = a.Kx2 + (NK == 2 ? bra.moff : 0);
-        if constexpr (sizeof(T) == 8) {
+        if constexpr (sizeof(T) == 8 && !kBlockDigestFP64) {
             for (int e = lane; e < nout; e += 32) {
                 const int ab = e / ncd, cd = e - ab * ncd;
                 const int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
@@ -408,12 +408,12 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 }
             }
         } else {
-            // FP32 quartets: weights in place (0 for non-canonical and
+            // Block digestion: weights in place (0 for non-canonical and
             // BF-screened elements), then one lane per J / K element the
-            // quartet touches sums its contributions (float products with the
-            // float density copies) and adds the sum to the FP64 accumulator:
-            // nab + ncd + na nc + na nd + nb nc + nb nd atomics per quartet
-            // instead of 6 per integral.
+            // quartet touches sums its contributions (FP32 quartets: float
+            // products with the float density copies) and adds the sum to the
+            // FP64 accumulator: nab + ncd + na nc + na nd + nb nc + nb nd
+            // atomics per quartet instead of 6 per integral.
             for (int e = lane; e < nout; e += 32) {
                 const int ab = e / ncd, cd = e - ab * ncd;
                 const int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
@@ -422,34 +422,35 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) ||
                                   (task.bra == task.ket && pij < pkl) ||
                                   (a.thr >= 0.0 && __ldg(Qbf + pij) * __ldg(Qbf + pkl) < a.thr);
-                const float f = (i == j ? 1.f : 2.f) * (k == l ? 1.f : 2.f) * (pij == pkl ? 1.f : 2.f);
+                const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
                 acc[e] = skip ? (T)0 : acc[e] * f;
             }
             __syncwarp();
             const int n0 = w_nc(bra.l0), n2 = w_nc(ket.l0);
             const int i0 = bra.bf0, j0 = bra.bf1, k0 = ket.bf0, l0 = ket.bf1;
-            const float* __restrict__ Dj32 = a.Dj32 + bra.moff;
-            auto d32 = [&](const float* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
-            auto put = [&](double* M, int r, int c, float v) {
-                if (v != 0.f) atomicAdd(M + (long long)r * K + c, (double)v);
+            const T* __restrict__ Dj32 = density_of<T>(a.Dj, a.Dj32) + bra.moff;
+            auto d32 = [&](const T* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
+            auto put = [&](double* M, int r, int c, T v) {
+                if (v != (T)0) atomicAdd(M + (long long)r * K + c, (double)v);
             };
             for (int ab = lane; ab < nab; ab += 32) {
-                float sj = 0.f;
+                T sj = 0;
                 for (int cd = 0; cd < ncd; ++cd) sj += d32(Dj32, k0 + cd / n3, l0 + cd % n3) * acc[ab * ncd + cd];
                 put(J, i0 + ab / n1, j0 + ab % n1, sj);
             }
             for (int cd = lane; cd < ncd; cd += 32) {
-                float sj = 0.f;
+                T sj = 0;
                 for (int ab = 0; ab < nab; ++ab) sj += d32(Dj32, i0 + ab / n1, j0 + ab % n1) * acc[ab * ncd + cd];
                 put(J, k0 + cd / n3, l0 + cd % n3, sj);
             }
             for (int sp = 0; sp < NK; ++sp) {
-                const float* __restrict__ Dk32 = (sp == 0 ? a.Dk32 : a.Dk232) + bra.moff;
+                const T* __restrict__ Dk32 =
+                    (sp == 0 ? density_of<T>(a.Dk, a.Dk32) : density_of<T>(a.Dk2, a.Dk232)) + bra.moff;
                 double* KK = sp == 0 ? Kx : Kx2;
                 // K_ik += D_jl v over (b, d)
                 for (int q = lane; q < n0 * n2; q += 32) {
                     const int ia = q / n2, ic = q - ia * n2;
-                    float s = 0.f;
+                    T s = 0;
                     for (int ib = 0; ib < n1; ++ib)
                         for (int id = 0; id < n3; ++id)
                             s += d32(Dk32, j0 + ib, l0 + id) * acc[(ia * n1 + ib) * ncd + ic * n3 + id];
@@ -458,7 +459,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 // K_jl += D_ik v over (a, c)
                 for (int q = lane; q < n1 * n3; q += 32) {
                     const int ib = q / n3, id = q - ib * n3;
-                    float s = 0.f;
+                    T s = 0;
                     for (int ia = 0; ia < n0; ++ia)
                         for (int ic = 0; ic < n2; ++ic)
                             s += d32(Dk32, i0 + ia, k0 + ic) * acc[(ia * n1 + ib) * ncd + ic * n3 + id];
@@ -467,7 +468,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 // K_il += D_jk v over (b, c)
                 for (int q = lane; q < n0 * n3; q += 32) {
                     const int ia = q / n3, id = q - ia * n3;
-                    float s = 0.f;
+                    T s = 0;
                     for (int ib = 0; ib < n1; ++ib)
                         for (int ic = 0; ic < n2; ++ic)
                             s += d32(Dk32, j0 + ib, k0 + ic) * acc[(ia * n1 + ib) * ncd + ic * n3 + id];
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 // K_jk += D_il v over (a, d)
                 for (int q = lane; q < n1 * n2; q += 32) {
                     const int ib = q / n2, ic = q - ib * n2;
-                    float s = 0.f;
+                    T s = 0;
                     for (int ia = 0; ia < n0; ++ia)
                         for (int id = 0; id < n3; ++id)
                             s += d32(Dk32, i0 + ia, l0 + id) * acc[(ia * n1 + ib) * ncd + ic * n3 + id];
