@@ -227,6 +227,10 @@ def run_engine(args):
 
     for _ in range(args.warmup):
         solve_resident()
+    # launch shape (chunk sizes, warps per CTA) from the autotuner, at the
+    # converged density of the warm-up solves; untimed setup
+    shape, _ = fb.autotune_launch_shape(dens, builds=2)
+    solve_resident()
     lat = []
     iters = builds = 0
     E_val = None
@@ -281,7 +285,9 @@ def run_engine(args):
         Kd = Pd.shape[0]
         fbm = H.FockBuilder(config=cfg_d, basis_set="6-31G*", device=local)
         tau, dE_proxy, _, _ = fbm.autotune_fp32_threshold(Pd, 2.5e-7)
+        shape_mx, _ = fbm.autotune_launch_shape(Pd, builds=2)
         fb64 = H.FockBuilder(config=cfg_d, basis_set="6-31G*", device=local)
+        shape_64, _ = fb64.autotune_launch_shape(Pd, builds=2)
         dPd = torch.tensor(Pd, device="cuda", dtype=torch.float64)
         dG64 = torch.zeros_like(dPd)
         dGmx = torch.zeros_like(dPd)
@@ -300,6 +306,7 @@ def run_engine(args):
         rmx = H.rhf_diis(cfg_d, "6-31G*", precision=H.HFX_PREC_MIXED, fp32_threshold=tau, **scf_kw)
         mixed = {"workload": "n-decane C10H22 RHF/6-31G* (K=%d), seed 20261203 noise 0.05 bohr" % Kd,
                  "fp32_threshold": tau, "autotune_target_dE": 2.5e-7, "autotune_dE": dE_proxy,
+                 "launch_shape_fp64": shape_64, "launch_shape_mixed": shape_mx,
                  "fock_builds_per_s_fp64": 1e3 / tms["fp64"], "fock_builds_per_s_mixed": 1e3 / tms["mixed"],
                  "speedup": tms["fp64"] / tms["mixed"], "fp32_quartet_fraction": smx["quartets_fp32"] / smx["quartets"],
                  "max_dF_vs_fp64": max_dF, "scf_dE_vs_fp64": rmx["E_tot"] - r64["E_tot"],
@@ -353,7 +360,8 @@ def run_engine(args):
         "ms_per_step": t_total / args.steps * 1e3 / max(1, 1), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "molecule": "benzene D6h (C r=2.6379, H r=4.68 bohr)", "basis": basis,
-                   "K": K, "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between steps (512 MB)"},
+                   "K": K, "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between steps (512 MB)",
+                   "launch_shape": shape},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},

@@ -168,6 +168,24 @@ class FockBuilder:
                                               ctypes.byref(a), ctypes.byref(b)))
         return t.value, d.value, a.value, b.value
 
+    def launch_shape(self):
+        s = _lib.LaunchShape()
+        check(lib.hfx_get_launch_shape(self._job, ctypes.byref(s)))
+        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps)
+
+    def set_launch_shape(self, small_chunk=256, warp_chunk=4096, warp_max_warps=8):
+        s = _lib.LaunchShape(small_chunk, warp_chunk, warp_max_warps)
+        check(lib.hfx_set_launch_shape(self._job, ctypes.byref(s)))
+
+    def autotune_launch_shape(self, P, builds=2):
+        """Coordinate search over the launch shape at density P; the job keeps
+        the fastest.  Returns (shape dict, best build ms)."""
+        P = self._mat(P)
+        s = _lib.LaunchShape()
+        ms = ctypes.c_double()
+        check(lib.hfx_autotune_launch_shape(self._job, ptr(P), int(builds), ctypes.byref(s), ctypes.byref(ms)))
+        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps), ms.value
+
     def stats(self):
         s = _lib.BuildStats()
         check(lib.hfx_last_build_stats(self._job, ctypes.byref(s)))

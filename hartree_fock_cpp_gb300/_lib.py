@@ -48,6 +48,11 @@ class BuildStats(ctypes.Structure):
                 ("flops_fp32", ctypes.c_double), ("launches", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
+class LaunchShape(ctypes.Structure):
+    _fields_ = [("small_chunk", ctypes.c_int), ("warp_chunk", ctypes.c_int), ("warp_max_warps", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
+
+
 class ScfOptions(ctypes.Structure):
     _fields_ = [("max_iterations", ctypes.c_int), ("epsilon", ctypes.c_double), ("damping", ctypes.c_double),
                 ("screening_threshold", ctypes.c_double), ("energy_threshold", ctypes.c_double),
@@ -127,6 +132,9 @@ SIGNATURES = {
     "hfx_job_rhf": (I, [V, V, V, V, V, V, V]),
     "hfx_job_uhf": (I, [V, V, I, I, V, V, V, V, V]),
     "hfx_last_build_stats": (I, [V, V]),
+    "hfx_get_launch_shape": (I, [V, V]),
+    "hfx_set_launch_shape": (I, [V, V]),
+    "hfx_autotune_launch_shape": (I, [V, V, I, V, P(D)]),
     "hfx_autotune_fp32_threshold": (I, [V, V, D, P(D), P(D), P(D), P(D)]),
     "hfx_rhf_diis": (I, [V, V, V, V, V, V, V]),
     "hfx_uhf_diis": (I, [V, V, I, I, V, V, V, V, V, V, V]),

@@ -269,6 +269,32 @@ hfx_status hfx_autotune_fp32_threshold(hfx_job* job, const double* P, double tar
     });
 }
 
+hfx_status hfx_get_launch_shape(const hfx_job* job, hfx_launch_shape* shape)
+{
+    return guarded([&] {
+        if (!job || !shape) throw Error(HFX_ERR_INVALID, "null argument");
+        *shape = job->job->launch_shape();
+    });
+}
+
+hfx_status hfx_set_launch_shape(hfx_job* job, const hfx_launch_shape* shape)
+{
+    return guarded([&] {
+        if (!job || !shape) throw Error(HFX_ERR_INVALID, "null argument");
+        job->job->set_launch_shape(*shape);
+    });
+}
+
+hfx_status hfx_autotune_launch_shape(hfx_job* job, const double* P, int builds, hfx_launch_shape* shape,
+                                     double* best_ms)
+{
+    return guarded([&] {
+        if (!job || !P) throw Error(HFX_ERR_INVALID, "null argument");
+        const double ms = job->job->autotune_launch_shape(P, builds, shape);
+        if (best_ms) *best_ms = ms;
+    });
+}
+
 hfx_status hfx_last_build_stats(const hfx_job* job, hfx_build_stats* stats)
 {
     return guarded([&] {

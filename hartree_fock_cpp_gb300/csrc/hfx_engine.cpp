@@ -108,9 +108,6 @@ void cuda_check(cudaError_t e, const char* what)
     }
 }
 
-// primitive quartets per thread-level chunk of a shell quartet
-constexpr long long kChunkPrims = 256;
-
 static double flops_per_prim(int la, int lb, int lc, int ld)
 {
     // algorithmic MD flop count per primitive quartet (boys + R + ket + bra + prefactor)
@@ -616,8 +613,9 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             const bool sm = is_small_class(pcb, pck, f32);
             Bucket& bk = sm ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
             // split the bra primitive pairs so that a chunk holds at most
-            // kChunkPrims primitive quartets (per thread) or 16x that (per warp)
-            const long long cap = sm ? kChunkPrims : 16LL * kChunkPrims;
+            // shape_.small_chunk primitive quartets (per thread) or
+            // shape_.warp_chunk (per warp)
+            const long long cap = sm ? shape_.small_chunk : shape_.warp_chunk;
             const long long pq = (long long)b.npp * k.npp;
             const int nch = (int)std::min<long long>(b.npp, std::max<long long>(1, (pq + cap - 1) / cap));
             for (int c = 0; c < nch; ++c) {
@@ -688,7 +686,8 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * k.npp;
             }
             g.slice = (slice + 1) & ~1;
-            g.warps_per_cta = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - kWarpSmemHeader) / (g.slice * elem[f])));
+            g.warps_per_cta = (int)std::max<size_t>(
+                1, std::min<size_t>((size_t)shape_.warp_max_warps, (200 * 1024 - kWarpSmemHeader) / (g.slice * elem[f])));
             size_t sm = kWarpSmemHeader + elem[f] * (size_t)g.slice * g.warps_per_cta;
             int ctas_per_sm = (int)std::max<size_t>(1, (228 * 1024) / (sm + 1024));
             long long need = ((long long)g.n + g.warps_per_cta - 1) / g.warps_per_cta;
@@ -1042,6 +1041,64 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
     cuda_check(cudaEventRecord(ev1_, stream_), "event");
     cuda_check(cudaStreamSynchronize(stream_), "fock build");
     record_stats((int)plan(mixed()).groups.size() + 1);
+}
+
+void Job::set_launch_shape(const hfx_launch_shape& s)
+{
+    if (s.small_chunk < 16 || s.small_chunk > 65536 || s.warp_chunk < 16 || s.warp_chunk > (1 << 20) ||
+        s.warp_max_warps < 1 || s.warp_max_warps > 8)
+        throw Error(HFX_ERR_INVALID, "launch shape out of range");
+    shape_ = s;
+    build_jk_groups(false, gs_fp64_);
+    if (mixed()) build_jk_groups(true, gs_mixed_);
+    d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
+}
+
+// Coordinate search over the launch shape: for each parameter in turn (small
+// chunk, warp chunk, warps per CTA), try its candidates with the others held,
+// keep the fastest; each trial times the job's own plan (mixed when the job
+// is mixed) at density P on the device, the best of `builds` builds.
+double Job::autotune_launch_shape(const double* P, int builds, hfx_launch_shape* out)
+{
+    const size_t n = (size_t)nmat();
+    DevBuf<double> dP, dG;
+    dP.alloc(n);
+    dG.alloc(n);
+    cuda_check(cudaMemcpyAsync(dP.p, P, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "H2D P");
+    builds = std::max(1, std::min(builds, 10));
+    auto trial = [&](const hfx_launch_shape& s) {
+        set_launch_shape(s);
+        double best = 1e30;
+        fock_rhf_device_ex(dP.p, dG.p, mixed(), 0.0);   // first build of the plan (eager)
+        for (int b = 0; b < builds; ++b) {
+            fock_rhf_device_ex(dP.p, dG.p, mixed(), 0.0);
+            best = std::min(best, (double)stats.kernel_ms);
+        }
+        return best;
+    };
+    hfx_launch_shape cur = shape_;
+    double cur_ms = trial(cur);
+    static const int small_c[] = {64, 128, 256, 512, 1024};
+    static const int warp_c[] = {1024, 2048, 4096, 8192, 16384};
+    static const int wpc_c[] = {2, 4, 8};
+    for (int param = 0; param < 3; ++param) {
+        const int* c = param == 0 ? small_c : param == 1 ? warp_c : wpc_c;
+        const int nc = param == 2 ? 3 : 5;
+        for (int i = 0; i < nc; ++i) {
+            hfx_launch_shape s = cur;
+            int& field = param == 0 ? s.small_chunk : param == 1 ? s.warp_chunk : s.warp_max_warps;
+            if (field == c[i]) continue;
+            field = c[i];
+            const double ms = trial(s);
+            if (ms < cur_ms * 0.99) {
+                cur = s;
+                cur_ms = ms;
+            }
+        }
+    }
+    set_launch_shape(cur);
+    if (out) *out = cur;
+    return cur_ms;
 }
 
 double Job::autotune_fp32_threshold(const double* P, double target_dE, double* dE_out, double* ms64, double* msmx)

@@ -243,6 +243,11 @@ public:
     // supplied by the caller; allocates nothing.  Jacc/Kacc hold K*K doubles,
     // counters num_launch_groups() ints.
     void fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, double* Kacc, int* counters);
+    // launch shape of the plans (chunk sizes, warps per CTA); setting it rebuilds the plans
+    const hfx_launch_shape& launch_shape() const { return shape_; }
+    void set_launch_shape(const hfx_launch_shape& s);
+    // pick the launch shape by timing builds at density P (host, K x K); returns the best build ms
+    double autotune_launch_shape(const double* P, int builds, hfx_launch_shape* out);
     int num_launch_groups() const { return (int)plan(true).groups.size(); }
     void fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb);
     void fock_rhf(const double* P, double* G);
@@ -297,6 +302,7 @@ private:
     DevBuf<long long> d_fmoff_;     // per molecule matrix offset
     DevBuf<unsigned char> d_active_;   // packed jobs: per molecule build flag
     bool packed_ = false;              // built by the packed (several-molecule) constructor
+    hfx_launch_shape shape_{256, 4096, 8, {0, 0, 0, 0, 0}};
 
     std::vector<HostPair> hpairs_;
     GroupSet gs_fp64_, gs_mixed_;

@@ -163,6 +163,27 @@ typedef struct {
 
 hfx_status hfx_last_build_stats(const hfx_job *job, hfx_build_stats *stats);
 
+/* Launch shape of a job's Fock-build plans: primitive quartets per task of
+ * the thread-per-quartet kernels (small_chunk) and of the warp kernel
+ * (warp_chunk; heavily contracted quartets are split into chunks of bra
+ * primitive pairs), and the warp kernel's maximum warps per CTA (1..8).
+ * Defaults 256 / 4096 / 8. */
+typedef struct {
+    int small_chunk;
+    int warp_chunk;
+    int warp_max_warps;
+    int reserved[5];
+} hfx_launch_shape;
+
+hfx_status hfx_get_launch_shape(const hfx_job *job, hfx_launch_shape *shape);
+hfx_status hfx_set_launch_shape(hfx_job *job, const hfx_launch_shape *shape);
+/* Autotuner: coordinate search over the three parameters, timing the job's
+ * own plan (mixed when the job is mixed) at density P (host K x K) with the
+ * best of `builds` device builds per trial; the job keeps the fastest shape.
+ * best_ms: its kernel time. */
+hfx_status hfx_autotune_launch_shape(hfx_job *job, const double *P, int builds, hfx_launch_shape *shape,
+                                     double *best_ms);
+
 /* Autotune the mixed-precision cut for this job: at density P (K*K host, e.g.
  * a converged or near-converged density), build G in FP64 and then in mixed
  * precision for tau = 0.3, 0.1, 0.03, ... 1e-5, keep the largest tau with

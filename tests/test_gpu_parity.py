@@ -222,3 +222,25 @@ def test_one_electron_gpu_matches_host_and_oracle(cfg, basis):
         g = _gold("water_sto3g.json")
         for key, M in (("S", S1), ("T", T1), ("V", V1)):
             assert np.abs(np.array(g[key]).reshape(M.shape) - M).max() < 1e-10
+
+
+# ---------------- launch-shape autotuner ----------------
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_launch_shape_autotuner_keeps_results(precision):
+    """Every launch shape computes the same G (chunking only regroups the
+    primitive sums); the autotuner returns a shape in range and the job keeps it."""
+    cfg = W.benzene()
+    with H.FockBuilder(config=cfg, basis_set="6-31G*", precision=precision, fp32_threshold=1e-2) as fb:
+        P = _sym(fb.K, 31) * 0.05
+        G0 = fb.repulsion_matrix(P)
+        shape, ms = fb.autotune_launch_shape(P, builds=1)
+        assert ms > 0 and fb.launch_shape() == shape
+        assert shape["small_chunk"] in (64, 128, 256, 512, 1024)
+        assert shape["warp_chunk"] in (1024, 2048, 4096, 8192, 16384)
+        assert shape["warp_max_warps"] in (2, 4, 8)
+        G1 = fb.repulsion_matrix(P)
+        assert np.abs(G1 - G0).max() < (1e-11 if precision == 0 else 1e-6)
+        fb.set_launch_shape(64, 1024, 2)
+        G2 = fb.repulsion_matrix(P)
+        assert np.abs(G2 - G0).max() < (1e-11 if precision == 0 else 1e-6)
