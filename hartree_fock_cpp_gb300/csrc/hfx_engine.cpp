@@ -199,12 +199,7 @@ void Job::init(const hfx_options& opt)
     cuda_check(cudaEventCreate(&evk1_), "event");
     d_counter_.alloc(4);
 
-    // Boys table F_m(k/16), m < kBoysM
-    std::vector<double> tab((size_t)kBoysN * kBoysM);
-    for (int k = 0; k < kBoysN; ++k) {
-        for (int m = 0; m < kBoysM - 1; ++m) tab[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
-        tab[(size_t)k * kBoysM + kBoysM - 1] = std::exp(-(double)k / kBoysInvStep);
-    }
+    const std::vector<double>& tab = boys_table_host();
     d_boys_.upload(tab, stream_);
     std::vector<float> tab32(tab.begin(), tab.end());
     d_boys32_.upload(tab32, stream_);
@@ -258,6 +253,44 @@ Job::~Job()
     for (auto st : aux_) cudaStreamDestroy(st);
     if (fork_ev_) cudaEventDestroy(fork_ev_);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+const std::vector<double>& boys_table_host()
+{
+    // F_m(k/16) for m < kBoysM - 1 (converged series) and exp(-k/16) in the
+    // last column; computed once per process (~70 ms of long-double series)
+    static const std::vector<double> tab = [] {
+        std::vector<double> t((size_t)kBoysN * kBoysM);
+        for (int k = 0; k < kBoysN; ++k) {
+            for (int m = 0; m < kBoysM - 1; ++m) t[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
+            t[(size_t)k * kBoysM + kBoysM - 1] = std::exp(-(double)k / kBoysInvStep);
+        }
+        return t;
+    }();
+    return tab;
+}
+
+// Task order of a launch group: largest cost first, so that the work queues
+// hand out the long tasks early.  Counting sort on quarter-octave cost bins
+// (stable within a bin): O(n), where an exact comparison sort of a
+// million-task plan took tens of milliseconds of job setup.
+static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost)
+{
+    constexpr int kBins = 256;
+    const size_t n = cost.size();
+    std::vector<unsigned char> bin(n);
+    std::vector<size_t> count(kBins + 1, 0);
+    for (size_t i = 0; i < n; ++i) {
+        const double c = cost[i] > 1.0 ? cost[i] : 1.0;
+        int b = (int)(4.0 * std::log2(c));
+        b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
+        bin[i] = (unsigned char)(kBins - 1 - b);   // descending cost = ascending bin
+        ++count[bin[i] + 1];
+    }
+    for (int b = 0; b < kBins; ++b) count[b + 1] += count[b];
+    std::vector<size_t> idx(n);
+    for (size_t i = 0; i < n; ++i) idx[count[bin[i]]++] = i;
+    return idx;
 }
 
 bool is_small_class(int pcb, int pck, bool fp32)
@@ -628,12 +661,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();
     gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
-    auto sorted = [](Bucket& bk) {
-        std::vector<size_t> idx(bk.t.size());
-        std::iota(idx.begin(), idx.end(), 0);
-        std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return bk.cost[x] > bk.cost[y]; });
-        return idx;
-    };
+    auto sorted = [](Bucket& bk) { return order_by_cost_desc(bk.cost); };
     for (int f = 0; f < 2; ++f)
         for (int pcb = 0; pcb < 10; ++pcb)
             for (int pck = 0; pck <= pcb; ++pck) {

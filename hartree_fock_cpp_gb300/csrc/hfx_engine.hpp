@@ -30,6 +30,8 @@ cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice,
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
 int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
 bool is_small_class(int pcb, int pck, bool fp32);
+// Boys table of the kernels ([kBoysN][kBoysM], last column exp(-T_k)), built once per process.
+const std::vector<double>& boys_table_host();
 
 void cuda_check(cudaError_t e, const char* what);
 

@@ -31,7 +31,6 @@
 
 namespace hfx {
 
-double boys_host(int m, double T);
 
 namespace {
 
@@ -273,11 +272,7 @@ const double* boys_table(int device)
     std::lock_guard<std::mutex> lk(mu);
     auto it = tabs.find(device);
     if (it != tabs.end()) return it->second;
-    std::vector<double> tab((size_t)kBoysN * kBoysM);
-    for (int k = 0; k < kBoysN; ++k) {
-        for (int m = 0; m < kBoysM - 1; ++m) tab[(size_t)k * kBoysM + m] = boys_host(m, (double)k / kBoysInvStep);
-        tab[(size_t)k * kBoysM + kBoysM - 1] = std::exp(-(double)k / kBoysInvStep);
-    }
+    const std::vector<double>& tab = boys_table_host();
     double* d = nullptr;
     cuda_check(cudaMalloc(&d, tab.size() * sizeof(double)), "boys table");
     cuda_check(cudaMemcpy(d, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice), "boys table");
