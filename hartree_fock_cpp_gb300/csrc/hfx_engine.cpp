@@ -271,20 +271,21 @@ const std::vector<double>& boys_table_host()
 }
 
 // Task order of a launch group: largest cost first, so that the work queues
-// hand out the long tasks early.  Counting sort on quarter-octave cost bins
-// (stable within a bin): O(n), where an exact comparison sort of a
-// million-task plan took tens of milliseconds of job setup.
+// hand out the long tasks early and the threads of a warp get tasks of about
+// the same cost.  Counting sort on 1/16-octave cost bins (stable within a
+// bin): O(n), where a comparison sort of a million-task plan took tens of
+// milliseconds of job setup.
 static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost)
 {
-    constexpr int kBins = 256;
+    constexpr int kBins = 1024;
     const size_t n = cost.size();
-    std::vector<unsigned char> bin(n);
+    std::vector<unsigned short> bin(n);
     std::vector<size_t> count(kBins + 1, 0);
     for (size_t i = 0; i < n; ++i) {
         const double c = cost[i] > 1.0 ? cost[i] : 1.0;
-        int b = (int)(4.0 * std::log2(c));
+        int b = (int)(16.0 * std::log2(c));
         b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
-        bin[i] = (unsigned char)(kBins - 1 - b);   // descending cost = ascending bin
+        bin[i] = (unsigned short)(kBins - 1 - b);   // descending cost = ascending bin
         ++count[bin[i] + 1];
     }
     for (int b = 0; b < kBins; ++b) count[b + 1] += count[b];
