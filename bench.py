@@ -367,6 +367,9 @@ def run_engine(args):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},
+        "eri_rate": {"shell_quartets_per_s": s["quartets"] / (kernel_ms * 1e-3),
+                     "primitive_quartets_per_s": s["prim_quartets"] / (kernel_ms * 1e-3),
+                     "shell_quartets_per_build": s["quartets"], "note": "surviving (Schwarz-screened) quartets of one FP64 build"},
         "mixed_precision": mixed,
         "served_stream": served,
         "batched_scans": scans,
