@@ -71,7 +71,8 @@ class ScfResult(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("max_active", ctypes.c_int), ("hbm_budget_gb", ctypes.c_double), ("device", ctypes.c_int),
-                ("precision", ctypes.c_int), ("fp32_threshold", ctypes.c_double), ("reserved", ctypes.c_int * 8)]
+                ("precision", ctypes.c_int), ("fp32_threshold", ctypes.c_double), ("pack_max", ctypes.c_int),
+                ("reserved", ctypes.c_int * 7)]
 
 
 class Request(ctypes.Structure):

@@ -30,6 +30,7 @@
 #include <thread>
 #include <tuple>
 
+#include "hfx_batch.hpp"
 #include "hfx_dscf.hpp"
 #include "hfx_engine.hpp"
 
@@ -229,6 +230,57 @@ double now_s()
 
 }  // namespace
 
+PackedRunStats run_packed(const std::vector<Basis>& bases, const hfx_options& jo, int nspin,
+                          const std::vector<PackedMember>& members, int max_parallel, const PackedDone& done)
+{
+    const int n = (int)bases.size();
+    if (n == 0) return PackedRunStats{};
+    if ((int)members.size() != n) throw Error(HFX_ERR_INVALID, "packed run: one member spec per molecule");
+    const double t0 = now_s();
+    Job job(bases, jo);
+    PackedBuilder builder(job, nspin);
+    const double t_setup = now_s() - t0;
+    const int workers = std::max(1, std::min({n, max_parallel > 0 ? max_parallel : n, 256}));
+    std::atomic<int> next{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto worker = [&] {
+        cudaSetDevice(dev);
+        for (int i = next++; i < n; i = next++) {
+            bool joined = false;
+            try {
+                const PackedMember& m = members[i];
+                ScfSetup setup = scf_setup(bases[i], true);
+                BatchMember member(builder, i, bases[i].K, job.mixed());
+                DeviceScf d(member, setup, nspin);
+                builder.join();
+                joined = true;
+                ScfOutput out = d.run(bases[i], setup, m.scf, m.n_alpha, m.n_beta, nullptr, nullptr, kBatchDeltaThr,
+                                      m.ctl);
+                builder.leave();
+                joined = false;
+                done(i, &out, out.converged ? HFX_OK : HFX_ERR_NOT_CONVERGED, std::string());
+            } catch (const Error& e) {
+                if (joined) builder.leave();
+                done(i, nullptr, e.code, e.what());
+            } catch (const std::exception& e) {
+                if (joined) builder.leave();
+                done(i, nullptr, HFX_ERR_CUDA, e.what());
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 0; w < workers; ++w) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    PackedRunStats st;
+    st.setup_s = t_setup;
+    st.builds = builder.builds();
+    st.build_ms = builder.build_ms();
+    st.quartets = job.stats.quartets;
+    st.flops_fp64 = job.stats.flops_fp64;
+    return st;
+}
+
 }  // namespace hfx
 
 using namespace hfx;
@@ -254,58 +306,33 @@ extern "C" hfx_status hfx_batch_scf(const hfx_molecule* mols, int n, const int* 
         jo.screening_threshold = o.screening_threshold;
         jo.precision = o.precision;
         jo.fp32_threshold = o.fp32_threshold;
-        Job job(bases, jo);
-        PackedBuilder builder(job, nspin);
-        const double t_setup = now_s() - t0;
-
-        const int workers = std::max(1, std::min({n, b.max_parallel > 0 ? b.max_parallel : n, 256}));
-        std::atomic<int> next{0};
+        std::vector<PackedMember> members(n);
+        for (int i = 0; i < n; ++i) {
+            members[i].scf = o;
+            members[i].n_alpha = nspin == 2 ? n_alpha[i] : 0;
+            members[i].n_beta = nspin == 2 ? n_beta[i] : 0;
+        }
         std::vector<hfx_status> status(n, HFX_OK);
         std::vector<std::string> msg(n);
-        int dev = 0;
-        cudaGetDevice(&dev);
-        auto worker = [&] {
-            cudaSetDevice(dev);
-            for (int i = next++; i < n; i = next++) {
-                bool joined = false;
-                try {
-                    ScfSetup setup = scf_setup(bases[i], true);
-                    BatchMember member(builder, i, bases[i].K, job.mixed());
-                    DeviceScf d(member, setup, nspin);
-                    builder.join();
-                    joined = true;
-                    ScfOutput out = d.run(bases[i], setup, o, nspin == 2 ? n_alpha[i] : 0, nspin == 2 ? n_beta[i] : 0,
-                                          nullptr, nullptr, kBatchDeltaThr);
-                    builder.leave();
-                    joined = false;
-                    fill(out, &results[i]);
-                    if (!out.converged) status[i] = HFX_ERR_NOT_CONVERGED;
-                } catch (const Error& e) {
-                    if (joined) builder.leave();
-                    std::memset(&results[i], 0, sizeof(results[i]));
-                    status[i] = e.code;
-                    msg[i] = e.what();
-                } catch (const std::exception& e) {
-                    if (joined) builder.leave();
-                    std::memset(&results[i], 0, sizeof(results[i]));
-                    status[i] = HFX_ERR_CUDA;
-                    msg[i] = e.what();
-                }
-            }
-        };
-        std::vector<std::thread> pool;
-        for (int w = 0; w < workers; ++w) pool.emplace_back(worker);
-        for (auto& t : pool) t.join();
-
+        const PackedRunStats rs =
+            run_packed(bases, jo, nspin, members, b.max_parallel,
+                       [&](int i, ScfOutput* out, hfx_status st, const std::string& m) {
+                           if (out)
+                               fill(*out, &results[i]);
+                           else
+                               std::memset(&results[i], 0, sizeof(results[i]));
+                           status[i] = st;
+                           msg[i] = m;
+                       });
         if (stats) {
             std::memset(stats, 0, sizeof(*stats));
             stats->seconds = now_s() - t0;
-            stats->setup_seconds = t_setup;
-            stats->cycles = builder.builds();
+            stats->setup_seconds = rs.setup_s;
+            stats->cycles = rs.builds;
             stats->molecules = n;
-            stats->build_ms = builder.build_ms();
-            stats->quartets = job.stats.quartets;
-            stats->flops_fp64 = job.stats.flops_fp64;
+            stats->build_ms = rs.build_ms;
+            stats->quartets = rs.quartets;
+            stats->flops_fp64 = rs.flops_fp64;
         }
         hfx_status worst = HFX_OK;
         for (int i = 0; i < n; ++i) {

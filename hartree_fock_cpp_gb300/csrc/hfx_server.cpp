@@ -12,6 +12,12 @@
 // step overlaps the others' GPU work.  Jobs finish, free their slot and
 // budget, and queued requests are admitted in their place.
 //
+// Packed mode (pack_max > 1): a worker that admits a request also admits up
+// to pack_max - 1 further queued requests of the same method and precision,
+// and runs them in lockstep on one packed job (run_packed, hfx_batch.cpp):
+// every SCF cycle is one Fock build for all of them.  Each job leaves the
+// pack, posts its result and frees its budget as soon as its own SCF ends.
+//
 // Failures stay with the job that caused them: a bad basis file, an
 // unsupported element, a footprint above the whole budget, an allocation
 // failure, a cancellation or a timeout ends that job with its status code.
@@ -28,6 +34,7 @@
 #include <thread>
 #include <vector>
 
+#include "hfx_batch.hpp"
 #include "hfx_dscf.hpp"
 #include "hfx_engine.hpp"
 #include "hfx_scf.hpp"
@@ -240,9 +247,31 @@ private:
                 }
                 if (!j) continue;
                 ++running_;
-                max_concurrent_ = std::max(max_concurrent_, running_);
                 j->state = HFX_JOB_RUNNING;
                 j->t_admit = now_s();
+                if (opt_.pack_max > 1) {
+                    std::vector<std::shared_ptr<ServerJob>> pack{j};
+                    for (auto it = queue_.begin(); it != queue_.end() && (int)pack.size() < opt_.pack_max;) {
+                        auto& c = *it;
+                        if (!c->cancel && c->method == j->method && c->precision == j->precision &&
+                            c->fp32_threshold == j->fp32_threshold) {
+                            c->state = HFX_JOB_RUNNING;
+                            c->t_admit = now_s();
+                            ++running_;
+                            pack.push_back(c);
+                            it = queue_.erase(it);
+                        } else {
+                            ++it;
+                        }
+                    }
+                    max_concurrent_ = std::max(max_concurrent_, running_);
+                    if (pack.size() > 1) {
+                        lk.unlock();
+                        run_pack(pack);
+                        continue;
+                    }
+                }
+                max_concurrent_ = std::max(max_concurrent_, running_);
             }
             run(j);
             {
@@ -272,6 +301,94 @@ private:
         }
         in_use_ += bytes;
         j.footprint = bytes;
+    }
+
+    // a job of a pack ends: result (or failure), budget and slot released
+    void finish_packed(ServerJob& j, ScfOutput* out, hfx_status st, const std::string& msg)
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            if (out) {
+                j.E_tot = out->E_tot;
+                j.iterations = out->iterations;
+                j.converged = out->converged;
+                j.fock_ms = out->fock_ms;
+                j.fock_builds = out->fock_builds;
+                j.Pa = std::move(out->P);
+                j.Pb = std::move(out->P2);
+                j.status = st;
+                j.state = HFX_JOB_DONE;
+            } else {
+                j.status = st;
+                j.message = msg;
+                j.state = HFX_JOB_FAILED;
+            }
+            --running_;
+            in_use_ -= j.footprint;
+            j.footprint = 0;
+            j.t_end = now_s();
+        }
+        done_cv_.notify_all();
+        cv_.notify_all();
+    }
+
+    void run_pack(const std::vector<std::shared_ptr<ServerJob>>& pack)
+    {
+        std::vector<std::shared_ptr<ServerJob>> live;
+        std::vector<Basis> bases;
+        for (auto& j : pack) {
+            try {
+                if (j->inject_fault == HFX_FAULT_SETUP) throw Error(HFX_ERR_INVALID, "injected fault during setup");
+                std::vector<const char*> syms;
+                for (auto& s : j->symbols) syms.push_back(s.c_str());
+                hfx_molecule mol{(int)syms.size(), syms.data(), j->xyz.data(), j->basis_set.c_str(),
+                                 j->basis_path.empty() ? nullptr : j->basis_path.c_str()};
+                Basis b = build_basis(mol);
+                j->K = b.K;
+                size_t fp = estimate_footprint(b);
+                if (j->inject_fault == HFX_FAULT_OOM) fp = budget_ + 1;
+                reserve(*j, fp);
+                if (j->inject_fault == HFX_FAULT_ALLOC) throw Error(HFX_ERR_OOM, "injected allocation failure");
+                bases.push_back(std::move(b));
+                live.push_back(j);
+            } catch (const Error& e) {
+                finish_packed(*j, nullptr, e.code, e.what());
+            } catch (const std::exception& e) {
+                finish_packed(*j, nullptr, HFX_ERR_INVALID, e.what());
+            }
+        }
+        if (live.empty()) return;
+        const ServerJob& first = *live[0];
+        hfx_options o{};
+        o.screening_threshold = first.scf.screening_threshold;
+        o.precision = first.precision;
+        o.fp32_threshold = first.fp32_threshold;
+        o.device = opt_.device;
+        std::vector<ScfControl> ctl(live.size());
+        std::vector<PackedMember> members(live.size());
+        for (size_t i = 0; i < live.size(); ++i) {
+            ServerJob& j = *live[i];
+            ctl[i] = ScfControl{&j.cancel, j.timeout_s > 0 ? j.t_submit + j.timeout_s : 0.0,
+                                j.inject_fault == HFX_FAULT_ITERATION ? 3 : 0};
+            members[i].scf = j.scf;
+            members[i].n_alpha = j.n_alpha;
+            members[i].n_beta = j.n_beta;
+            members[i].ctl = &ctl[i];
+        }
+        std::vector<char> ended(live.size(), 0);
+        try {
+            run_packed(bases, o, first.method == 1 ? 2 : 1, members, 0,
+                       [&](int i, ScfOutput* out, hfx_status st, const std::string& m) {
+                           ended[i] = 1;
+                           finish_packed(*live[i], out, st, m);
+                       });
+        } catch (const Error& e) {
+            for (size_t i = 0; i < live.size(); ++i)
+                if (!ended[i]) finish_packed(*live[i], nullptr, e.code, e.what());
+        } catch (const std::exception& e) {
+            for (size_t i = 0; i < live.size(); ++i)
+                if (!ended[i]) finish_packed(*live[i], nullptr, HFX_ERR_CUDA, e.what());
+        }
     }
 
     void run(std::shared_ptr<ServerJob> j)

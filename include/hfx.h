@@ -288,7 +288,10 @@ typedef struct {
     int device;
     int precision;           /* default precision of requests (HFX_PREC_*) */
     double fp32_threshold;   /* default mixed-precision cut */
-    int reserved[8];
+    int pack_max;            /* > 1: a worker admits up to pack_max queued requests of one method and
+                                precision together and runs them in lockstep on one packed job (one
+                                Fock build per SCF cycle for all of them); 0 or 1: one job per worker */
+    int reserved[7];
 } hfx_server_options;
 
 enum { HFX_JOB_QUEUED = 0, HFX_JOB_RUNNING = 1, HFX_JOB_DONE = 2, HFX_JOB_FAILED = 3 };

@@ -75,3 +75,25 @@ def test_cancel_queued_job():
         srv.drain(300)
         assert srv.poll(first)["converged"]
         assert srv.poll(second)["status"] == 7             # HFX_ERR_CANCELLED
+
+
+def test_packed_mode_results_same_alone_and_in_the_pack():
+    """pack_max > 1: requests of one method are admitted together and iterate in
+    lockstep on one packed job; each result equals the job run alone, and a
+    faulty request in the pack fails alone."""
+    rhf = [j for j in MIX if j["method"] == "RHF"]
+    alone = [_alone(j) for j in rhf]
+    with Server(max_active=2, pack_max=8) as srv:
+        ids = [srv.submit(**j) for j in rhf]
+        bad = srv.submit(config=W.water(), basis_set="6-31G*", inject_fault="iteration")
+        uhf = srv.submit(config=OH, basis_set="6-31G*", method="UHF", spin=(5, 4))
+        srv.drain(600)
+        infos = [srv.poll(i) for i in ids]
+        ib, iu = srv.poll(bad), srv.poll(uhf)
+    for j, a, inf in zip(rhf, alone, infos):
+        assert inf["state"] == "done", inf
+        assert inf["converged"]
+        assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL
+        assert abs(inf["iterations"] - a["iterations"]) <= 1
+    assert ib["state"] == "failed"
+    assert iu["state"] == "done" and iu["converged"]
