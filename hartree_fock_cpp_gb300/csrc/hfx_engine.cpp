@@ -587,7 +587,6 @@ void Job::for_each_surviving_quartet(double thr, F&& f) const
 void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops,
                       double* prims) const
 {
-    int np = (int)hpairs_.size();
     // order pairs so that the pair with the larger (L, l0) is the bra
     auto key = [&](int p) { return (hpairs_[p].l0 + hpairs_[p].l1) * 16 + hpairs_[p].l0; };
     std::vector<double> cost;
@@ -627,7 +626,6 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     clear_graphs();   // graphs hold the previous plan's task pointers
     const double thr = opt_.screening_threshold;
     const double tau = opt_.fp32_threshold;
-    const int np = (int)hpairs_.size();
     auto pcof = [&](int p) { return pair_class(hpairs_[p].l0, hpairs_[p].l1); };
     // buckets: small classes per (pcb, pck, fp32); warp classes per (fp32)
     struct Bucket {
@@ -901,7 +899,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
             } else {
                 SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys_.p,
                                     opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr,
-                                    active};
+                                    active, nullptr, nullptr, nullptr};
                 cuda_check(small_spec_f64(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
@@ -919,7 +917,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                    tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
-                                   Dsh, dthr, nullptr, nullptr, active};
+                                   Dsh, dthr, nullptr, nullptr, active, nullptr, nullptr, nullptr};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             }
@@ -1132,7 +1130,6 @@ double Job::autotune_launch_shape(const double* P, int builds, hfx_launch_shape*
 
 double Job::autotune_fp32_threshold(const double* P, double target_dE, double* dE_out, double* ms64, double* msmx)
 {
-    const int K = basis_.K;
     const size_t n = (size_t)nmat();
     std::vector<double> G64(n), Gm(n);
     fock_rhf_ex(P, G64.data(), false, 0.0);

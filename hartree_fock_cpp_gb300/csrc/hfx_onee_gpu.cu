@@ -45,12 +45,16 @@ struct OneeShell {
     int woff, pad;
 };
 
+struct Nucleus {
+    double x, y, z, Z;
+};
+
 struct OneeArgs {
     const OneeShell* sh;
     const double* exps;
     const double* w;        // per shell: w[c * nprim + i] = coefficient x cart_norm of component c
     const int2* pairs;      // (A, B), A >= B
-    const double4* nuc;     // (x, y, z, Z)
+    const Nucleus* nuc;
     int natom;
     const double* boys;     // [kBoysN][kBoysM], last column exp(-T_k)
     int K;
@@ -223,12 +227,12 @@ __global__ void __launch_bounds__(kOneeThreads) k_one_electron(OneeArgs a)
         for (int ab = 0; ab < nab; ++ab) vacc[ab] = 0.0;
         const int c1 = min(a.natom, (ch + 1) * kNucChunk);
         for (int c = ch * kNucChunk; c < c1; ++c) {
-            const double4 C = a.nuc[c];
+            const Nucleus C = a.nuc[c];
             const double X = Px - C.x, Y = Py - C.y, Z = Pz - C.z;
             double F[7], R[kMaxHerm];
             boys_rt(L, p * (X * X + Y * Y + Z * Z), a.boys, F);
             hermite_R_rt(L, p, X, Y, Z, F, R);
-            const double pref = -C.w * 2.0 * 3.14159265358979323846 / p;
+            const double pref = -C.Z * 2.0 * 3.14159265358979323846 / p;
             for (int ab = 0; ab < nab; ++ab) {
                 const int ca = ab / nb, cb = ab - ca * nb;
                 int ax, ay, az, bx, by, bz;
@@ -309,9 +313,9 @@ void one_electron_gpu(const Basis& b, std::vector<double>& S, std::vector<double
     for (int A = 0; A < ns; ++A)
         for (int B = 0; B <= A; ++B) pairs.push_back(make_int2(A, B));
     const int natom = (int)b.atom_Z.size();
-    std::vector<double4> nuc(std::max(1, natom));
+    std::vector<Nucleus> nuc(std::max(1, natom));
     for (int c = 0; c < natom; ++c)
-        nuc[c] = make_double4(b.atom_xyz[3 * c], b.atom_xyz[3 * c + 1], b.atom_xyz[3 * c + 2], (double)b.atom_Z[c]);
+        nuc[c] = Nucleus{b.atom_xyz[3 * c], b.atom_xyz[3 * c + 1], b.atom_xyz[3 * c + 2], (double)b.atom_Z[c]};
 
     cudaStream_t st;
     cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -319,7 +323,7 @@ void one_electron_gpu(const Basis& b, std::vector<double>& S, std::vector<double
         DevBuf<OneeShell> d_sh;
         DevBuf<double> d_exps, d_w, d_out;
         DevBuf<int2> d_pairs;
-        DevBuf<double4> d_nuc;
+        DevBuf<Nucleus> d_nuc;
         d_sh.upload(sh, st);
         d_exps.upload(exps, st);
         d_w.upload(w, st);
