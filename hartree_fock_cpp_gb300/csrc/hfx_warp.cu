@@ -272,20 +272,22 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                         recur_lane<T>(X, Y, Z, L, Sd + lane, 32, Ra + lane, 32, nbt, cft);
                     }
                     __syncwarp();
-                    // stage 2: W[tuv][cd] += sum_b sum_k (+-) c_k R_b[tuv + tnp_k]
+                    // stage 2: W[tuv][cd] += sum_k (+-) sum_b c_bk R_b[tuv + tnp_k]; the
+                    // coefficient's Hermite offset and sign are read once per k and
+                    // reused for the nb ket primitive pairs of this round
                     for (int e = lane; e < nw; e += 32) {
                         const int tuv = e / ncd, cd = e - tuv * ncd;
                         const int lt = clin[tuv];
                         const int k0 = __ldg(abs_k + cd), k1 = __ldg(abs_k + cd + 1);
+                        const T* ck0 = rec + ket.rec_off + (long long)kl0 * ck.stride + 5;
                         T s = (T)0;
-                        for (int b = 0; b < nb; ++b) {
-                            const T* ck_ = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride + 5;
-                            for (int k = k0; k < k1; ++k) {
-                                const int w = __ldg(kl_k + k);
-                                const T r = Ra[idx3[lt + (w & 16383)] * 32 + b];
-                                const T c = __ldg(ck_ + k);
-                                s = (w & 16384) ? w_fma(-c, r, s) : w_fma(c, r, s);
-                            }
+                        for (int k = k0; k < k1; ++k) {
+                            const int w = __ldg(kl_k + k);
+                            const T* Rk = Ra + idx3[lt + (w & 16383)] * 32;
+                            const T* ckk = ck0 + k;
+                            T t = (T)0;
+                            for (int b = 0; b < nb; ++b) t = w_fma(__ldg(ckk + (long long)b * ck.stride), Rk[b], t);
+                            s = (w & 16384) ? s - t : s + t;
                         }
                         W[e] += s;
                     }
