@@ -164,6 +164,9 @@ __device__ __forceinline__ long long wpidx(int a, int b)
     return (long long)hi * (hi + 1) / 2 + lo;
 }
 
+// ket primitive pairs per round of the level-parallel (non-lane) mode
+constexpr int kWarpKetRound = 4;
+
 template <typename T, int NK>
 __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
 {
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         T* W = acc + nout;
         T* Ra = W + nw;
         const bool lane_mode = a.lane_r && L <= 6 && ket.npp >= 6;
-        T* Sd = Ra + (lane_mode ? HL * 32 : 2 * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
+        T* Sd = Ra + (lane_mode ? HL * 32 : (2 + kWarpKetRound) * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
         for (int e = lane; e < nout; e += 32) acc[e] = (T)0;
 
         const int ij_end = task.ij >> 16;
@@ -294,44 +297,59 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                     __syncwarp();
                 }
             } else {
-                for (int kl = 0; kl < ket.npp; ++kl) {
-                    const T* rk = rec + ket.rec_off + (long long)kl * ck.stride;
-                    const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),
-                            rq = __ldg(rk + 4);
-                    const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
-                    const T rs = rsqrt(p + q);
-                    const T rho = p * q * (rs * rs);
-                    const T Tv = rho * (X * X + Y * Y + Z * Z);
-                    const T pref = (T)34.98683665524972 * rp * rq * rs;
-                    // seeds: lane 0 (downward recursion is sequential in m)
-                    if (lane == 0) boys_seeds<T>(Tv, rho, (p + q) * rp * rq, pref, L, a.boys, Sd, 1);
-                    __syncwarp();
-                    // level-parallel recursion, ping-pong between Ra and Rb
-                    T* prev = Ra;
-                    T* cur = Ra + HL;
-                    if (lane == 0) prev[0] = Sd[L];
-                    __syncwarp();
-                    for (int n = L - 1; n >= 0; --n) {
-                        const int cnt = w_nh(L - n);
-                        for (int e = lane; e < cnt; e += 32) {
-                            T val;
-                            if (e == 0) {
-                                val = Sd[n];
-                            } else {
-                                const int w = nbt[e];
-                                const int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511, c2 = (w >> 20) & 15;
-                                const T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
-                                val = xd * prev[i1];
-                                if (c2) val = w_fma(cft[e], prev[i2], val);
-                            }
-                            cur[e] = val;
+                // kNB ket primitive pairs per round: each one's R by the
+                // level-parallel recursion (ping-pong in Ra, last level into its
+                // slot of Rb), then one ket transform over the round that reads
+                // each coefficient's Hermite offset and sign once
+                T* Rb = Ra + 2 * HL;
+                for (int kl0 = 0; kl0 < ket.npp; kl0 += kWarpKetRound) {
+                    const int nb = min(kWarpKetRound, ket.npp - kl0);
+                    for (int b = 0; b < nb; ++b) {
+                        const T* rk = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride;
+                        const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),
+                                rq = __ldg(rk + 4);
+                        const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
+                        const T rs = rsqrt(p + q);
+                        const T rho = p * q * (rs * rs);
+                        const T Tv = rho * (X * X + Y * Y + Z * Z);
+                        const T pref = (T)34.98683665524972 * rp * rq * rs;
+                        // seeds: lane 0 (downward recursion is sequential in m)
+                        if (lane == 0) boys_seeds<T>(Tv, rho, (p + q) * rp * rq, pref, L, a.boys, Sd, 1);
+                        __syncwarp();
+                        T* slot = Rb + b * HL;
+                        T* prev = Ra;
+                        T* cur = Ra + HL;
+                        if (lane == 0) {
+                            if (L == 0)
+                                slot[0] = Sd[0];
+                            else
+                                prev[0] = Sd[L];
                         }
                         __syncwarp();
-                        T* tmp = prev;
-                        prev = cur;
-                        cur = tmp;
+                        for (int n = L - 1; n >= 0; --n) {
+                            const int cnt = w_nh(L - n);
+                            T* dst = n == 0 ? slot : cur;
+                            for (int e = lane; e < cnt; e += 32) {
+                                T val;
+                                if (e == 0) {
+                                    val = Sd[n];
+                                } else {
+                                    const int w = nbt[e];
+                                    const int dir = w & 3, i1 = (w >> 2) & 511, i2 = (w >> 11) & 511,
+                                              c2 = (w >> 20) & 15;
+                                    const T xd = dir == 0 ? X : (dir == 1 ? Y : Z);
+                                    val = xd * prev[i1];
+                                    if (c2) val = w_fma(cft[e], prev[i2], val);
+                                }
+                                dst[e] = val;
+                            }
+                            __syncwarp();
+                            T* tmp = prev;
+                            prev = cur;
+                            cur = tmp;
+                        }
                     }
-                    const T* ck_ = rk + 5;
+                    const T* ck0 = rec + ket.rec_off + (long long)kl0 * ck.stride + 5;
                     for (int e = lane; e < nw; e += 32) {
                         const int tuv = e / ncd, cd = e - tuv * ncd;
                         const int lt = clin[tuv];
@@ -339,9 +357,12 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                         T s = (T)0;
                         for (int k = k0; k < k1; ++k) {
                             const int w = __ldg(kl_k + k);
-                            const T r = prev[idx3[lt + (w & 16383)]];
-                            const T c = __ldg(ck_ + k);
-                            s = (w & 16384) ? w_fma(-c, r, s) : w_fma(c, r, s);
+                            const int ri = idx3[lt + (w & 16383)];
+                            const T* ckk = ck0 + k;
+                            T t = (T)0;
+                            for (int b = 0; b < nb; ++b)
+                                t = w_fma(__ldg(ckk + (long long)b * ck.stride), Rb[b * HL + ri], t);
+                            s = (w & 16384) ? s - t : s + t;
                         }
                         W[e] += s;
                     }
@@ -498,7 +519,7 @@ int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_
     int nab = w_nc(l0b) * w_nc(l1b), ncd = w_nc(l0k) * w_nc(l1k);
     int HL = w_nh(L);
     bool lane_mode = lane_r && L <= 6 && npp_ket >= 6;
-    int r = lane_mode ? HL * 32 + (L + 1) * 32 : 2 * HL + (L + 1);
+    int r = lane_mode ? HL * 32 + (L + 1) * 32 : (2 + kWarpKetRound) * HL + (L + 1);
     return nab * ncd + w_nh(L1) * ncd + r;
 }
 
