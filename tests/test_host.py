@@ -170,3 +170,42 @@ def test_errors_are_status_codes_not_exits():
     with pytest.raises(H.HfxError):
         H.rhf_diis(W.water(), "STO-3G", eri_device="TPU")
     assert "unsupported" in H._lib.last_error() or True
+
+
+def test_cube_file_layout(tmp_path):
+    """write_cube_file follows the reference's layout (cube.hpp:383-450):
+    2 comment lines, natoms + origin, 3 grid vectors, atoms, values z-fastest
+    six per line in %.8e."""
+    from hartree_fock_cpp_gb300 import cube
+    res = 3
+    field = np.arange(res ** 3, dtype=float) * 0.5
+    c = {"field": field, "origin": np.array([-1.0, -2.0, -3.0]), "dx": 0.25, "res": res}
+    atoms = [("O", (0.0, 0.0, 0.0)), ("H", (0.0, 1.4, 1.1))]
+    f = tmp_path / "x.cube"
+    cube.write_cube_file(str(f), c, atoms, comment="test")
+    lines = f.read_text().splitlines()
+    assert lines[0] == "test"
+    assert lines[2].split() == ["2", "-1", "-2", "-3"]
+    assert lines[3].split()[:2] == ["3", "0.25"]
+    assert lines[6].split()[0] == "8" and lines[7].split()[0] == "1"
+    vals = " ".join(lines[8:]).split()
+    assert len(vals) == res ** 3
+    assert float(vals[5]) == 2.5 and vals[0] == "0.00000000e+00"
+    assert len(lines[8].split()) == 6
+
+
+def test_oracle_grid_restatement_on_hand_values():
+    """The oracle's function_eval / electron_density restatement on a case
+    worked by hand: one normalised s function, P = [[2]] gives
+    rho(r) = 2 phi(r)^2 with phi(r) = N c exp(-a r^2)."""
+    import oracle as O
+    fb = O.FlatBasis([("H", (0.0, 0.0, 0.0))], "STO-3G")
+    pts = np.array([[0.0, 0.0, 0.0], [0.3, -0.2, 0.5]])
+    phi = O.basis_values(fb, pts)
+    r2 = (pts ** 2).sum(1)
+    ref = sum(fb.norm[i] * fb.coeff[i] * np.exp(-fb.alpha[i] * r2) for i in range(fb.prim_off[1]))
+    assert np.allclose(phi[0], ref, rtol=1e-14)
+    rho = O.electron_density(fb, [[2.0]], pts)
+    assert np.allclose(rho, 2.0 * ref ** 2, rtol=1e-14)
+    box = O.box_points((0.0, 0.0, 0.0), 2.0, 3)
+    assert box.shape == (27, 3) and np.allclose(box[1], [-1.0, -1.0, 0.0])
