@@ -171,10 +171,11 @@ class FockBuilder:
     def launch_shape(self):
         s = _lib.LaunchShape()
         check(lib.hfx_get_launch_shape(self._job, ctypes.byref(s)))
-        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps)
+        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps,
+                    lane_min_npp=s.lane_min_npp)
 
-    def set_launch_shape(self, small_chunk=256, warp_chunk=4096, warp_max_warps=8):
-        s = _lib.LaunchShape(small_chunk, warp_chunk, warp_max_warps)
+    def set_launch_shape(self, small_chunk=256, warp_chunk=4096, warp_max_warps=8, lane_min_npp=6):
+        s = _lib.LaunchShape(small_chunk, warp_chunk, warp_max_warps, lane_min_npp)
         check(lib.hfx_set_launch_shape(self._job, ctypes.byref(s)))
 
     def autotune_launch_shape(self, P, builds=2):
@@ -184,7 +185,8 @@ class FockBuilder:
         s = _lib.LaunchShape()
         ms = ctypes.c_double()
         check(lib.hfx_autotune_launch_shape(self._job, ptr(P), int(builds), ctypes.byref(s), ctypes.byref(ms)))
-        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps), ms.value
+        return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps,
+                    lane_min_npp=s.lane_min_npp), ms.value
 
     def stats(self):
         s = _lib.BuildStats()

@@ -50,7 +50,7 @@ class BuildStats(ctypes.Structure):
 
 class LaunchShape(ctypes.Structure):
     _fields_ = [("small_chunk", ctypes.c_int), ("warp_chunk", ctypes.c_int), ("warp_max_warps", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("lane_min_npp", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class ScfOptions(ctypes.Structure):

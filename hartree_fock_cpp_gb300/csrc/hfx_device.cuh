@@ -196,7 +196,7 @@ struct WarpArgs {
     double* Kx;
     double* Kx2;
     int slice;                 // per-warp shared-memory slice, in T elements
-    int lane_r;                // 1: lane-parallel R allowed for this launch
+    int lane_min_npp;          // lane-parallel R for L <= 6 and ket npp >= this (0: never)
     const double* Dsh;         // per shell pair max |D| (density screening), or null
     double dthr;               // skip a quartet when Q_AB Q_CD max|D| < dthr (0: never)
     double* Qout_bf;           // Schwarz pass (NK = 0): BF-pair bounds out

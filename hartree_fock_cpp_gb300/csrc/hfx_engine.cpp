@@ -500,7 +500,7 @@ void Job::compute_schwarz()
     std::map<int, int> tier_slice;
     for (int p = 0; p < np; ++p) {
         const HostPair& h = hpairs_[p];
-        int sl = warp_slice_elems(h.l0, h.l1, h.l0, h.l1, h.npp, true);
+        int sl = warp_slice_elems(h.l0, h.l1, h.l0, h.l1, h.npp, kDefaultLaneMinNpp);
         int tier = 0;
         while ((512 << tier) < sl) ++tier;
         tiers[tier].push_back({p, p, h.npp << 16});
@@ -533,7 +533,7 @@ void Job::compute_schwarz()
         a.thr = -1.0;
         a.K = basis_.K;
         a.slice = slice;
-        a.lane_r = 1;
+        a.lane_min_npp = kDefaultLaneMinNpp;
         a.Qout_bf = d_qbf_.p;
         a.Qout_sh = d_qsh_.p;
         cuda_check(launch_warp(false, &a, 0, grid, wpc, stream_), "schwarz launch");
@@ -692,7 +692,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             const HostPair& k = hpairs_[bk.t[i].ket];
             // tier by slice size (powers of two), so that tasks with small
             // slices are not held to the occupancy of the largest one
-            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true);
+            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, shape_.lane_min_npp);
             int tier = 0;
             while ((512 << tier) < sl) ++tier;
             tiers[tier].push_back(i);
@@ -707,12 +707,13 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             for (size_t i : kv.second) {
                 const HostPair& b = hpairs_[bk.t[i].bra];
                 const HostPair& k = hpairs_[bk.t[i].ket];
-                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, true));
+                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, shape_.lane_min_npp));
                 all.push_back(bk.t[i]);
                 g.flops += bk.cost[i];
                 g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * k.npp;
             }
             g.slice = (slice + 1) & ~1;
+            g.lane_min_npp = shape_.lane_min_npp;
             g.warps_per_cta = (int)std::max<size_t>(
                 1, std::min<size_t>((size_t)shape_.warp_max_warps, (200 * 1024 - kWarpSmemHeader) / (g.slice * elem[f])));
             size_t sm = kWarpSmemHeader + elem[f] * (size_t)g.slice * g.warps_per_cta;
@@ -909,14 +910,16 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
             if (g.fp32) {
                 WarpArgs<float> a{d_pairs_.p, d_rec32_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                   tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
-                                  opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                  opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
+                                  g.lane_min_npp,
                                   Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
                                    tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
-                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice, 1,
+                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
+                                   g.lane_min_npp,
                                    Dsh, dthr, nullptr, nullptr, active, nullptr, nullptr, nullptr};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
@@ -1073,7 +1076,7 @@ void Job::fock_rhf_device_scratch(const double* dP, double* dG, double* Jacc, do
 void Job::set_launch_shape(const hfx_launch_shape& s)
 {
     if (s.small_chunk < 16 || s.small_chunk > 65536 || s.warp_chunk < 16 || s.warp_chunk > (1 << 20) ||
-        s.warp_max_warps < 1 || s.warp_max_warps > 8)
+        s.warp_max_warps < 1 || s.warp_max_warps > 8 || s.lane_min_npp < 0)
         throw Error(HFX_ERR_INVALID, "launch shape out of range");
     shape_ = s;
     build_jk_groups(false, gs_fp64_);
@@ -1082,7 +1085,7 @@ void Job::set_launch_shape(const hfx_launch_shape& s)
 }
 
 // Coordinate search over the launch shape: for each parameter in turn (small
-// chunk, warp chunk, warps per CTA), try its candidates with the others held,
+// chunk, warp chunk, warps per CTA, lane-mode threshold), try its candidates with the others held,
 // keep the fastest; each trial times the job's own plan (mixed when the job
 // is mixed) at density P on the device, the best of `builds` builds.
 double Job::autotune_launch_shape(const double* P, int builds, hfx_launch_shape* out)
@@ -1108,12 +1111,16 @@ double Job::autotune_launch_shape(const double* P, int builds, hfx_launch_shape*
     static const int small_c[] = {64, 128, 256, 512, 1024};
     static const int warp_c[] = {1024, 2048, 4096, 8192, 16384};
     static const int wpc_c[] = {2, 4, 8};
-    for (int param = 0; param < 3; ++param) {
-        const int* c = param == 0 ? small_c : param == 1 ? warp_c : wpc_c;
-        const int nc = param == 2 ? 3 : 5;
+    static const int lane_c[] = {0, 6, 12, 24};
+    for (int param = 0; param < 4; ++param) {
+        const int* c = param == 0 ? small_c : param == 1 ? warp_c : param == 2 ? wpc_c : lane_c;
+        const int nc = param == 2 ? 3 : param == 3 ? 4 : 5;
         for (int i = 0; i < nc; ++i) {
             hfx_launch_shape s = cur;
-            int& field = param == 0 ? s.small_chunk : param == 1 ? s.warp_chunk : s.warp_max_warps;
+            int& field = param == 0 ? s.small_chunk
+                         : param == 1 ? s.warp_chunk
+                         : param == 2 ? s.warp_max_warps
+                                      : s.lane_min_npp;
             if (field == c[i]) continue;
             field = c[i];
             const double ms = trial(s);

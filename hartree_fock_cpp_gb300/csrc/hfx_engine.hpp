@@ -28,7 +28,10 @@ cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s);
 cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<float>)
 cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s);
 cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps_per_cta, cudaStream_t st);
-int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r);
+// shared-memory slice (elements) of a warp task; the lane-parallel R mode (L <= 6,
+// ket npp >= lane_min_npp, 0: never) needs 32 R vectors, the level-parallel one a round
+int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, int lane_min_npp);
+constexpr int kDefaultLaneMinNpp = 6;
 bool is_small_class(int pcb, int pck, bool fp32);
 // Boys table of the kernels ([kBoysN][kBoysM], last column exp(-T_k)), built once per process.
 const std::vector<double>& boys_table_host();
@@ -109,6 +112,7 @@ struct LaunchGroup {
     bool fp32;
     int slice;           // warp kernel: per-warp slice (elements)
     int warps_per_cta;
+    int lane_min_npp;    // warp kernel: lane-parallel R threshold the slice was sized for
     int grid;
     size_t off, n;       // task range in the concatenated list
     double flops, prims;
@@ -304,7 +308,7 @@ private:
     DevBuf<long long> d_fmoff_;     // per molecule matrix offset
     DevBuf<unsigned char> d_active_;   // packed jobs: per molecule build flag
     bool packed_ = false;              // built by the packed (several-molecule) constructor
-    hfx_launch_shape shape_{256, 4096, 8, {0, 0, 0, 0, 0}};
+    hfx_launch_shape shape_{256, 4096, 8, kDefaultLaneMinNpp, {0, 0, 0, 0}};
 
     std::vector<HostPair> hpairs_;
     GroupSet gs_fp64_, gs_mixed_;

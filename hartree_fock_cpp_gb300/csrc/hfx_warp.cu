@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         T* acc = sl;
         T* W = acc + nout;
         T* Ra = W + nw;
-        const bool lane_mode = a.lane_r && L <= 6 && ket.npp >= 6;
+        const bool lane_mode = a.lane_min_npp > 0 && L <= 6 && ket.npp >= a.lane_min_npp;
         T* Sd = Ra + (lane_mode ? HL * 32 : (2 + kWarpKetRound) * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
         for (int e = lane; e < nout; e += 32) acc[e] = (T)0;
 
@@ -514,12 +514,12 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
 }
 
 // slice size (T elements) a task needs
-int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, bool lane_r)
+int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, int lane_min_npp)
 {
     int L1 = l0b + l1b, L2 = l0k + l1k, L = L1 + L2;
     int nab = w_nc(l0b) * w_nc(l1b), ncd = w_nc(l0k) * w_nc(l1k);
     int HL = w_nh(L);
-    bool lane_mode = lane_r && L <= 6 && npp_ket >= 6;
+    bool lane_mode = lane_min_npp > 0 && L <= 6 && npp_ket >= lane_min_npp;
     int r = lane_mode ? HL * 32 + (L + 1) * 32 : (2 + kWarpKetRound) * HL + (L + 1);
     return nab * ncd + w_nh(L1) * ncd + r;
 }

@@ -166,18 +166,22 @@ hfx_status hfx_last_build_stats(const hfx_job *job, hfx_build_stats *stats);
 /* Launch shape of a job's Fock-build plans: primitive quartets per task of
  * the thread-per-quartet kernels (small_chunk) and of the warp kernel
  * (warp_chunk; heavily contracted quartets are split into chunks of bra
- * primitive pairs), and the warp kernel's maximum warps per CTA (1..8).
- * Defaults 256 / 4096 / 8. */
+ * primitive pairs), the warp kernel's maximum warps per CTA (1..8), and the
+ * smallest ket primitive-pair count for which the warp kernel computes the
+ * R integrals of 32 ket primitive pairs at once, one per lane (L <= 6 only;
+ * 0: never; otherwise all lanes work on one primitive pair at a time).
+ * Defaults 256 / 4096 / 8 / 6. */
 typedef struct {
     int small_chunk;
     int warp_chunk;
     int warp_max_warps;
-    int reserved[5];
+    int lane_min_npp;
+    int reserved[4];
 } hfx_launch_shape;
 
 hfx_status hfx_get_launch_shape(const hfx_job *job, hfx_launch_shape *shape);
 hfx_status hfx_set_launch_shape(hfx_job *job, const hfx_launch_shape *shape);
-/* Autotuner: coordinate search over the three parameters, timing the job's
+/* Autotuner: coordinate search over the four parameters, timing the job's
  * own plan (mixed when the job is mixed) at density P (host K x K) with the
  * best of `builds` device builds per trial; the job keeps the fastest shape.
  * best_ms: its kernel time. */

@@ -239,8 +239,10 @@ def test_launch_shape_autotuner_keeps_results(precision):
         assert shape["small_chunk"] in (64, 128, 256, 512, 1024)
         assert shape["warp_chunk"] in (1024, 2048, 4096, 8192, 16384)
         assert shape["warp_max_warps"] in (2, 4, 8)
+        assert shape["lane_min_npp"] in (0, 6, 12, 24)
         G1 = fb.repulsion_matrix(P)
         assert np.abs(G1 - G0).max() < (1e-11 if precision == 0 else 1e-6)
-        fb.set_launch_shape(64, 1024, 2)
-        G2 = fb.repulsion_matrix(P)
-        assert np.abs(G2 - G0).max() < (1e-11 if precision == 0 else 1e-6)
+        for lane in (0, 24):
+            fb.set_launch_shape(64, 1024, 2, lane)
+            G2 = fb.repulsion_matrix(P)
+            assert np.abs(G2 - G0).max() < (1e-11 if precision == 0 else 1e-6)
