@@ -106,8 +106,6 @@ __host__ __device__ inline int herm_index(int t, int u, int v)
     return off + u;
 }
 
-enum DigestMode { MODE_JK = 0, MODE_ERI = 1, MODE_SCHWARZ = 2 };
-
 // One unit of work: a shell quartet (bra pair, ket pair), restricted to the
 // bra primitive pairs [ij & 0xffff, ij >> 16).  Heavily contracted quartets
 // are split into several such chunks, each digested on its own (J and K are
@@ -118,33 +116,19 @@ struct Task {
     int ij;
 };
 
-// Work-list descriptor of one launch.
+// Arguments of the unique-ERI kernel (hfx_kernels.cu).
 struct LaunchArgs {
     const DPair* pairs;
     const PairGeo* pp_geo;
     const double* epool;
-    const float4* pp_geo32;
-    const float* epool32;
     const double* boys;      // [kBoysN][kBoysM]
-    const float* boys32;
     const Task* tasks;
     int ntasks;
     int* counter;            // work-queue head (zeroed before launch)
     int K;
     double thr;              // BF-level Schwarz threshold (< 0: none)
     const double* Qbf;
-    // MODE_JK
-    const double* Dj;        // density for J (RHF: P; UHF: Pa+Pb)
-    const double* Dk;        // density for K (RHF: P; UHF: Pa)
-    const double* Dk2;       // UHF: Pb (nullptr for RHF)
-    double* Jacc;
-    double* Kacc;
-    double* Kacc2;
-    // MODE_ERI
-    double* eri;
-    // MODE_SCHWARZ
-    double* Qout_bf;
-    unsigned long long* Qout_sh;
+    double* eri;             // packed unique ERIs, eri_index order
 };
 
 // Arguments of the small-class (thread-per-shell-quartet) kernels.

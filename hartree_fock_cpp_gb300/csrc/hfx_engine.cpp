@@ -472,8 +472,7 @@ LaunchArgs Job::base_args() const
     return a;
 }
 
-void Job::run_tasks(int mode, int nk, const std::vector<Task>*, const DevBuf<Task>& tasks, int ntasks, int maxacc,
-                    int maxw, int maxr, LaunchArgs a)
+void Job::run_eri_tasks(const DevBuf<Task>& tasks, int ntasks, int maxacc, int maxw, int maxr, LaunchArgs a)
 {
     if (ntasks == 0) return;
     a.tasks = tasks.p;
@@ -482,7 +481,7 @@ void Job::run_tasks(int mode, int nk, const std::vector<Task>*, const DevBuf<Tas
     size_t sm = generic_smem_bytes(maxacc, maxw, maxr);
     int per_sm = (int)std::max<size_t>(1, std::min<size_t>(16, (220 * 1024) / std::max<size_t>(sm, 1)));
     int grid = std::min(ntasks, nsm_ * per_sm);
-    cuda_check(launch_generic(mode, nk, a, maxacc, maxw, maxr, grid, stream_), "quartet kernel launch");
+    cuda_check(launch_eri(a, maxacc, maxw, maxr, grid, stream_), "ERI kernel launch");
 }
 
 void Job::compute_schwarz()
@@ -1272,7 +1271,7 @@ void Job::eri_unique(double thr, double* out)
     LaunchArgs a = base_args();
     a.thr = thr;
     a.eri = d_out.p;
-    run_tasks(MODE_ERI, 1, &tasks, dt, (int)tasks.size(), maxacc, maxw, maxr, a);
+    run_eri_tasks(dt, (int)tasks.size(), maxacc, maxw, maxr, a);
     cuda_check(cudaMemcpyAsync(out, d_out.p, nq * sizeof(double), cudaMemcpyDeviceToHost, stream_), "D2H");
     cuda_check(cudaStreamSynchronize(stream_), "eri_unique");
 }

@@ -15,8 +15,7 @@ namespace hfx {
 
 // device launch helpers (hfx_kernels.cu)
 size_t generic_smem_bytes(int maxacc, int maxw, int maxr);
-cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
-                           cudaStream_t st);
+cudaError_t launch_eri(const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid, cudaStream_t st);
 // symmetrisation of packed accumulators: one grid row (blockIdx.y) per
 // molecule, Kmax = the largest molecule's K
 KernelSpec finish_rhf_spec(int Kmax, int nfrag);   // k_finish_rhf(Jacc, Kacc, G, fk, fmoff, active)
@@ -269,8 +268,7 @@ private:
     void compute_schwarz();
     void build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& maxw, int& maxr, double* flops = nullptr,
                      double* prims = nullptr) const;
-    void run_tasks(int mode, int nk, const std::vector<Task>* host_tasks, const DevBuf<Task>& tasks, int ntasks,
-                   int maxacc, int maxw, int maxr, LaunchArgs a);
+    void run_eri_tasks(const DevBuf<Task>& tasks, int ntasks, int maxacc, int maxw, int maxr, LaunchArgs a);
     LaunchArgs base_args() const;
     template <typename F>
     void for_each_surviving_quartet(double thr, F&& f) const;

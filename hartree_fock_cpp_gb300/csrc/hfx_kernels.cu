@@ -128,11 +128,12 @@ __device__ __forceinline__ long long pair_idx(int a, int b)
     return (long long)hi * (hi + 1) / 2 + lo;
 }
 
-// Generic shell-quartet kernel: one CTA (128 threads) per shell quartet,
-// quartets taken from a global work queue.  MODE selects the digestion;
-// NK = 1 (RHF: J, K) or 2 (UHF: J, Ka, Kb).
-template <int MODE, int NK>
-__global__ void __launch_bounds__(128) k_quartet_generic(LaunchArgs a, int maxacc, int maxw, int maxr)
+// Unique-ERI kernel (the ERI_GPU replacement): one CTA (128 threads) per
+// shell quartet, quartets taken from a global work queue, dense E matrices,
+// every canonical BF-level integral written to its packed eri_index slot
+// (zero stays where the BF-level Schwarz test fails).  The Fock builds and the
+// Schwarz pass run on the class kernels instead.
+__global__ void __launch_bounds__(128) k_quartet_eri(LaunchArgs a, int maxacc, int maxw, int maxr)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     short* idx3 = reinterpret_cast<short*>(smem);            // 13^3 shorts
@@ -217,40 +218,13 @@ __global__ void __launch_bounds__(128) k_quartet_generic(LaunchArgs a, int maxac
             int ab = e / ncd, cd = e - ab * ncd;
             int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
             int i = bra.bf0 + ia, j = bra.bf1 + ib, k = ket.bf0 + ic, l = ket.bf1 + id;
-            double v = acc[e];
-            if (MODE == MODE_SCHWARZ) {
-                if (ab == cd && (!bra.same || ia >= ib)) {
-                    double qv = sqrt(v > 0.0 ? v : 0.0);
-                    a.Qout_bf[pair_idx(i, j)] = qv;
-                    atomicMax(a.Qout_sh + task.bra, (unsigned long long)__double_as_longlong(qv));
-                }
-                continue;
-            }
             if (bra.same && ia < ib) continue;
             if (ket.same && ic < id) continue;
             long long pij = pair_idx(i, j), pkl = pair_idx(k, l);
             if (task.bra == task.ket && pij < pkl) continue;
             if (a.thr >= 0.0 && a.Qbf[pij] * a.Qbf[pkl] < a.thr) continue;
-            if (MODE == MODE_ERI) {
-                long long hi = pij > pkl ? pij : pkl, lo = pij > pkl ? pkl : pij;
-                a.eri[hi * (hi + 1) / 2 + lo] = v;
-                continue;
-            }
-            double f = (i == j ? 1.0 : 2.0) * (k == l ? 1.0 : 2.0) * (pij == pkl ? 1.0 : 2.0);
-            v *= f;
-            const int K = a.K;
-            atomicAdd(a.Jacc + (long long)i * K + j, a.Dj[(long long)k * K + l] * v);
-            atomicAdd(a.Jacc + (long long)k * K + l, a.Dj[(long long)i * K + j] * v);
-            atomicAdd(a.Kacc + (long long)i * K + k, a.Dk[(long long)j * K + l] * v);
-            atomicAdd(a.Kacc + (long long)j * K + l, a.Dk[(long long)i * K + k] * v);
-            atomicAdd(a.Kacc + (long long)i * K + l, a.Dk[(long long)j * K + k] * v);
-            atomicAdd(a.Kacc + (long long)j * K + k, a.Dk[(long long)i * K + l] * v);
-            if (NK == 2) {
-                atomicAdd(a.Kacc2 + (long long)i * K + k, a.Dk2[(long long)j * K + l] * v);
-                atomicAdd(a.Kacc2 + (long long)j * K + l, a.Dk2[(long long)i * K + k] * v);
-                atomicAdd(a.Kacc2 + (long long)i * K + l, a.Dk2[(long long)j * K + k] * v);
-                atomicAdd(a.Kacc2 + (long long)j * K + k, a.Dk2[(long long)i * K + l] * v);
-            }
+            long long hi = pij > pkl ? pij : pkl, lo = pij > pkl ? pkl : pij;
+            a.eri[hi * (hi + 1) / 2 + lo] = acc[e];
         }
         __syncthreads();
     }
@@ -356,20 +330,13 @@ static cudaError_t allow_max_smem_generic(K kern)
     return err;
 }
 
-cudaError_t launch_generic(int mode, int nk, const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid,
-                           cudaStream_t st)
+cudaError_t launch_eri(const LaunchArgs& a, int maxacc, int maxw, int maxr, int grid, cudaStream_t st)
 {
     size_t sm = generic_smem_bytes(maxacc, maxw, maxr);
-    auto go = [&](auto kern) -> cudaError_t {
-        cudaError_t e = allow_max_smem_generic(kern);
-        if (e != cudaSuccess) return e;
-        kern<<<grid, 128, sm, st>>>(a, maxacc, maxw, maxr);
-        return cudaGetLastError();
-    };
-    if (mode == MODE_SCHWARZ) return go(k_quartet_generic<MODE_SCHWARZ, 1>);
-    if (mode == MODE_ERI) return go(k_quartet_generic<MODE_ERI, 1>);
-    if (nk == 2) return go(k_quartet_generic<MODE_JK, 2>);
-    return go(k_quartet_generic<MODE_JK, 1>);
+    cudaError_t e = allow_max_smem_generic(k_quartet_eri);
+    if (e != cudaSuccess) return e;
+    k_quartet_eri<<<grid, 128, sm, st>>>(a, maxacc, maxw, maxr);
+    return cudaGetLastError();
 }
 
 // Grid-stride elementwise kernels: 256 threads, at most 1024 CTAs per grid row.
