@@ -235,7 +235,12 @@ void Job::init(const hfx_options& opt)
         }
     }
     build_jk_groups(false, gs_fp64_);
-    if (mixed()) build_jk_groups(true, gs_mixed_);
+    if (mixed()) {
+        build_jk_groups(true, gs_mixed_);
+        // float density copies of the FP32 groups, allocated with the job so
+        // that builds (the allocation-free entry point included) allocate nothing
+        d_d32_.alloc((size_t)3 * nmat());
+    }
     d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
     cuda_check(cudaStreamSynchronize(stream_), "job setup");
 }
@@ -1146,6 +1151,7 @@ double Job::autotune_fp32_threshold(const double* P, double target_dE, double* d
     const int prec0 = opt_.precision;
     const double tau0 = opt_.fp32_threshold;
     opt_.precision = HFX_PREC_MIXED;
+    d_d32_.alloc((size_t)3 * nmat());
     for (double tau : cand) {
         opt_.fp32_threshold = tau;
         build_jk_groups(true, gs_mixed_);
