@@ -8,7 +8,9 @@
 // flight, since cudaMalloc can synchronise the device.  This entry point
 // keeps every scratch buffer of the build (the J and K accumulators and the
 // work-queue counters) in one file-scope __device__ array, so its only
-// device writes besides the caller's output are into that array.
+// device writes besides the caller's output are into that array and, for a
+// mixed-precision job, into the float density copies the job allocated when
+// it was created.
 //
 // Limits: K <= kNoAllocMaxK basis functions and at most kNoAllocMaxGroups
 // kernel launch groups per build; larger jobs are rejected with
