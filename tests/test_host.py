@@ -209,3 +209,29 @@ def test_oracle_grid_restatement_on_hand_values():
     assert np.allclose(rho, 2.0 * ref ** 2, rtol=1e-14)
     box = O.box_points((0.0, 0.0, 0.0), 2.0, 3)
     assert box.shape == (27, 3) and np.allclose(box[1], [-1.0, -1.0, 0.0])
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct of include/hfx.h has the same size in the ctypes mirror
+    (a compiled probe prints sizeof and the offset of the last member)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    from hartree_fock_cpp_gb300 import _lib as L
+    pairs = {"hfx_functions": L.Functions, "hfx_molecule": L.Molecule, "hfx_options": L.Options,
+             "hfx_build_stats": L.BuildStats, "hfx_launch_shape": L.LaunchShape, "hfx_scf_options": L.ScfOptions,
+             "hfx_scf_result": L.ScfResult, "hfx_server_options": L.ServerOptions, "hfx_request": L.Request,
+             "hfx_job_info": L.JobInfo, "hfx_server_stats_t": L.ServerStats, "hfx_batch_options": L.BatchOptions,
+             "hfx_batch_stats": L.BatchStats}
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "hfx.h"\nint main(void) {\n' +
+                   "".join('    printf("%s %%zu\\n", sizeof(%s));\n' % (n, n) for n in pairs) + "    return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run([gcc, "-I", os.path.join(repo, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    sizes = {l.split()[0]: int(l.split()[1]) for l in out if l.strip()}
+    for name, cls in pairs.items():
+        assert sizes[name] == ctypes.sizeof(cls), name
