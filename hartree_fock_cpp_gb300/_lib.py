@@ -143,6 +143,7 @@ SIGNATURES = {
     "hfx_uhf_diis_with_builder": (I, [V, V, I, I, JK_BUILDER, V, V, V, V]),
     "hfx_build_functions": (I, [V, P(I), P(I), V, V, V, V, V, V]),
     "hfx_debug_pair_data": (I, [V, P(I), P(I), P(ctypes.c_longlong), V, V, V]),
+    "hfx_debug_packed_pairs": (I, [V, I, P(I), V, V]),
     "hfx_one_electron": (I, [V, V, V, V, P(I)]),
     "hfx_one_electron_gpu": (I, [V, I, V, V, V, P(I)]),
     "hfx_grid_density": (I, [V, I, V, V, D, I, V]),

@@ -479,6 +479,32 @@ hfx_status hfx_uhf_diis_with_builder(const hfx_molecule* mol, const hfx_scf_opti
     });
 }
 
+hfx_status hfx_debug_packed_pairs(const hfx_molecule* mols, int n, int* npairs, int* rec, long long* offs)
+{
+    return guarded([&] {
+        if (!mols || n <= 0) throw Error(HFX_ERR_INVALID, "null molecules or n <= 0");
+        std::vector<Basis> bases;
+        for (int i = 0; i < n; ++i) bases.push_back(build_basis(mols[i]));
+        Fragments fr;
+        const Basis all = concat_basis(bases, fr);
+        const PairData pd = build_pair_data(all, fr);
+        if (npairs) *npairs = (int)pd.dpairs.size();
+        for (size_t p = 0; p < pd.dpairs.size(); ++p) {
+            const DPair& d = pd.dpairs[p];
+            if (rec) {
+                int* r = rec + 10 * p;
+                r[0] = d.frag; r[1] = d.kdim; r[2] = d.pbase; r[3] = d.id; r[4] = d.sh0;
+                r[5] = d.sh1; r[6] = d.bf0; r[7] = d.bf1; r[8] = d.l0; r[9] = d.l1;
+            }
+            if (offs) {
+                offs[3 * p] = d.moff;
+                offs[3 * p + 1] = d.qoff;
+                offs[3 * p + 2] = d.npp;
+            }
+        }
+    });
+}
+
 hfx_status hfx_one_electron(const hfx_molecule* mol, double* S, double* T, double* V, int* K)
 {
     return guarded([&] {

@@ -275,6 +275,11 @@ hfx_status hfx_build_functions(const hfx_molecule *mol, int *K, int *nprim_total
  * epool = the dense E[ab][tuv] blocks.  Query sizes with NULL arrays. */
 hfx_status hfx_debug_pair_data(const hfx_molecule *mol, int *npairs, int *nprimpairs, long long *nepool, int *rec,
                                double *geo, double *epool);
+/* Test hook (host only, no device work): the shell-pair records of a packed
+ * job over n molecules.  Per pair, rec[10*p ..] = frag, kdim, pbase, id, sh0,
+ * sh1, bf0, bf1, l0, l1 (shell and function indices local to the molecule)
+ * and offs[3*p ..] = moff, qoff, npp.  Pass rec = offs = NULL to get npairs. */
+hfx_status hfx_debug_packed_pairs(const hfx_molecule *mols, int n, int *npairs, int *rec, long long *offs);
 
 /* One-electron matrices S, T, V of a molecule (integrals.hpp:10-536), host. */
 hfx_status hfx_one_electron(const hfx_molecule *mol, double *S, double *T, double *V, int *K);

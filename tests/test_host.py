@@ -235,3 +235,47 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
     sizes = {l.split()[0]: int(l.split()[1]) for l in out if l.strip()}
     for name, cls in pairs.items():
         assert sizes[name] == ctypes.sizeof(cls), name
+
+
+def test_packed_job_layout():
+    """Packed jobs (several molecules in one job): shell pairs never mix
+    molecules, indices are molecule-local, each molecule's pairs start at
+    its pair base with the single-molecule order, and its matrices and
+    Schwarz table sit at the running sums of K^2 and K(K+1)/2."""
+    mols = [(W.water(), "6-31G*"), (W.nacl_scan(8)[3], "cc-pVTZ"), ([("H", (0, 0, 0)), ("H", (0, 0, 1.4))], "STO-3G")]
+    args = [_lib.MoleculeArgs(c, b) for c, b in mols]
+    arr = (_lib.Molecule * len(args))(*[a.c for a in args])
+    n = ctypes.c_int()
+    _lib.check(_lib.lib.hfx_debug_packed_pairs(ctypes.cast(arr, ctypes.c_void_p), len(args), ctypes.byref(n), None,
+                                               None))
+    rec = np.zeros(10 * n.value, dtype=np.int32)
+    offs = np.zeros(3 * n.value, dtype=np.int64)
+    _lib.check(_lib.lib.hfx_debug_packed_pairs(ctypes.cast(arr, ctypes.c_void_p), len(args), None, _lib.ptr(rec),
+                                               _lib.ptr(offs)))
+    rec = rec.reshape(-1, 10)
+    offs = offs.reshape(-1, 3)
+    Ks = [H.basis_construction(c, b).K for c, b in mols]
+    moff, qoff, pbase = 0, 0, 0
+    for f, (cfg, bs) in enumerate(mols):
+        sel = np.where(rec[:, 0] == f)[0]
+        # the single-molecule pair records of this molecule
+        m = _lib.MoleculeArgs(cfg, bs)
+        npp, nprim, nep = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _lib.check(_lib.lib.hfx_debug_pair_data(m.ref(), ctypes.byref(npp), ctypes.byref(nprim), ctypes.byref(nep),
+                                                None, None, None))
+        single = np.zeros(10 * npp.value, dtype=np.int32)
+        _lib.check(_lib.lib.hfx_debug_pair_data(m.ref(), None, None, None, _lib.ptr(single), None, None))
+        single = single.reshape(-1, 10)
+        assert len(sel) == npp.value
+        assert sel[0] == pbase and np.all(np.diff(sel) == 1)
+        assert np.all(rec[sel, 1] == Ks[f]) and np.all(rec[sel, 2] == pbase)
+        assert np.all(rec[sel, 3] == sel)                                   # global pair id
+        assert np.all(rec[sel, 6] == single[:, 0]) and np.all(rec[sel, 7] == single[:, 1])   # local bf0, bf1
+        assert np.all(rec[sel, 8] == single[:, 2]) and np.all(rec[sel, 9] == single[:, 3])   # l0, l1
+        assert np.all(rec[sel, 6] < Ks[f]) and np.all(rec[sel, 7] < Ks[f])
+        assert np.all(offs[sel, 0] == moff) and np.all(offs[sel, 1] == qoff)
+        assert np.all(offs[sel, 2] == single[:, 5])                         # primitive pairs
+        moff += Ks[f] ** 2
+        qoff += Ks[f] * (Ks[f] + 1) // 2
+        pbase += len(sel)
+    assert pbase == n.value
