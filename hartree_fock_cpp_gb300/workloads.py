@@ -101,8 +101,6 @@ def random_molecule(rng, n_heavy, max_tries=200):
         for _try in range(max_tries):
             parent = int(rng.integers(0, len(atoms)))
             ps = atoms[parent][0]
-            if len(bonds[parent]) >= VALENCE[ps] - (0 if len(atoms) > 1 else 0) - (1 if ps in ("O", "S") and len(bonds[parent]) >= 1 and False else 0):
-                continue
             if len(bonds[parent]) >= VALENCE[ps]:
                 continue
             kind = kinds[int(rng.choice(4, p=probs))]

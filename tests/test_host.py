@@ -279,3 +279,31 @@ def test_packed_job_layout():
         qoff += Ks[f] * (Ks[f] + 1) // 2
         pbase += len(sel)
     assert pbase == n.value
+
+
+def test_served_stream_properties():
+    """The seeded served stream: 2..24 heavy atoms from {C,N,O,S}, H-capped,
+    ~80% RHF / 20% UHF doublets (n_alpha = n_beta + 1), bases at about
+    0.3 / 0.4 / 0.3, no two atoms closer than 2.0 bohr except an H and its
+    parent (bond 1.9..2.5 bohr), and the same stream for the same seed."""
+    jobs = W.served_stream(300)
+    assert W.served_stream(5) == jobs[:5]
+    n_uhf = sum(j["method"] == "UHF" for j in jobs)
+    assert 0.12 < n_uhf / len(jobs) < 0.28
+    frac = {b: sum(j["basis"] == b for j in jobs) / len(jobs) for b in ("STO-3G", "6-31G*", "cc-pVDZ")}
+    assert abs(frac["STO-3G"] - 0.3) < 0.08 and abs(frac["6-31G*"] - 0.4) < 0.08 and abs(frac["cc-pVDZ"] - 0.3) < 0.08
+    for j in jobs[:80]:
+        syms = [s for s, _ in j["config"]]
+        heavy = [s for s in syms if s != "H"]
+        assert 2 <= len(heavy) <= 24 and set(heavy) <= {"C", "N", "O", "S"}
+        xyz = np.array([p for _, p in j["config"]])
+        d = np.linalg.norm(xyz[:, None, :] - xyz[None, :, :], axis=-1)
+        close = np.argwhere(np.triu(d < 2.0 - 1e-9, 1))
+        for a, b in close:
+            assert (syms[a] == "H") != (syms[b] == "H"), (syms[a], syms[b], d[a, b])
+            assert d[a, b] >= 1.9 - 1e-9
+        if j["method"] == "UHF":
+            na, nb = j["spin"]
+            assert na == nb + 1 and na + nb == W.n_electrons(j["config"])
+        else:
+            assert W.n_electrons(j["config"]) % 2 == 0
