@@ -159,23 +159,47 @@ def cpu_baseline(config, basis, iterations, sample_quartets, nthreads, seed=2026
     O.repulsion_matrix(P, eri_dummy)
     t_contract = time.perf_counter() - t0
     t_solve = t_tensor + iterations * t_contract
-    return dict(value=1.0 / t_solve, unit=UNIT, cores=nthreads, kind="port",
+    return dict(value=1.0 / t_solve, unit=UNIT, cores=nthreads, kind="port", K=K,
                 sample="%d random unique BF quartets of %d (%.1f%% survive 1e-8 screening) on %d threads, "
                        "plus one O(K^4) repulsion_matrix; extrapolated: tensor %.1f s + %d x %.2f s contraction"
                        % (sample_quartets, nq, 100 * frac, nthreads, t_tensor, iterations, t_contract),
                 seconds_per_solve=t_solve, sample_seconds=t_sample + t_contract + t_schwarz)
 
 
+def load_workloads():
+    """The synthetic workload generators, loaded from their file (numpy only):
+    importing the package would load the engine's library into the process."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("hfx_workloads",
+                                                  os.path.join(REPO, "hartree_fock_cpp_gb300", "workloads.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def reference_iterations():
+    """SCF iterations of the headline workload in the reference's own loop:
+    the oracle's rhf_diis (scf.hpp:205-419) over the tensor of the reference's
+    integrals.hpp compiled unchanged (tests/golden/scf_golden.json)."""
+    with open(os.path.join(REPO, "tests", "golden", "scf_golden.json")) as f:
+        return int(json.load(f)["benzene_ccpvdz"]["iterations"])
+
+
+def workload_config(K, ws):
+    """The config dict of the headline workload, the same in both arms."""
+    return {"workload": WORKLOAD, "molecule": "benzene D6h (C r=2.6379, H r=4.68 bohr)", "basis": "cc-pVDZ",
+            "K": K, "parallelism": "replicas" if ws > 1 else "single",
+            "l2": "GPU arm: flushed between steps (512 MB write)"}
+
+
 def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    from hartree_fock_cpp_gb300 import workloads as W
+    W = load_workloads()
     nthreads = os.cpu_count() or 1
     cfg = W.benzene()
-    # SCF iterations of this workload at these settings: 23 (the engine's
-    # solve, which reproduces the reference SCF's iteration count within +-1)
-    iters = 23
+    iters = reference_iterations()
     vals = []
     base = None
     for s in range(args.warmup + args.steps):
@@ -189,7 +213,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "impl": "reference CPU algorithm (oracle port), host threads"},
+            "config": workload_config(base["K"], ws),
+            "reference_impl": "reference CPU algorithm (oracle port of integrals.hpp repulsion_tensor + "
+                              "linalg.hpp repulsion_matrix), host threads, %d SCF iterations of the reference "
+                              "loop" % iters,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": base["kind"],
                              "sample": base["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -207,6 +234,10 @@ def run_engine(args):
     from hartree_fock_cpp_gb300 import _lib, workloads as W
 
     fp64_peak, fp32_peak = H.measure_peaks(local)
+    try:
+        dmma_peak = H.measure_dmma_peak(local)
+    except Exception:  # noqa: BLE001 - reported as unmeasured
+        dmma_peak = None
     cfg = W.benzene()
     basis = "cc-pVDZ"
     scf_kw = dict(epsilon=1e-7, energy_threshold=1e-8)
@@ -279,7 +310,8 @@ def run_engine(args):
     peak = fp64_peak / 1e3
 
     # ---- mixed vs FP64 Fock builds on n-decane/6-31G* ------------------------
-    mixed = None if args.no_mixed else section(mixed_section, H, W, torch, flush, args, local, scf_kw)
+    mixed = None if args.no_mixed else section(mixed_section, H, W, torch, flush, args, local, scf_kw,
+                                                          (fp64_peak, fp32_peak))
 
     # ---- served request stream: continuous batching vs one-at-a-time FP64 ----
     served = section(serve_section, H, W, args.serve_jobs, local) if args.serve_jobs > 0 else None
@@ -290,7 +322,7 @@ def run_engine(args):
     # ---- e2e: through hfx_rhf_diis with host buffers -------------------------
     e2e_lat = []
     r = None
-    for k in range(1 + max(1, min(args.steps, 3))):
+    for k in range(1 + args.steps):
         t0 = time.perf_counter()
         r = H.rhf_diis(cfg, basis, **scf_kw)
         dt = time.perf_counter() - t0
@@ -312,39 +344,79 @@ def run_engine(args):
             torch.distributed.barrier()
         return
     cpu = None
+    ref_iters = None
+    try:
+        ref_iters = reference_iterations()
+    except Exception:  # noqa: BLE001 - fixture absent: the engine's own count
+        pass
     if ws == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        b = cpu_baseline(cfg, basis, iters, sample_quartets=2000 * nthreads, nthreads=nthreads)
+        b = cpu_baseline(cfg, basis, ref_iters or iters, sample_quartets=2000 * nthreads, nthreads=nthreads)
         cpu = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t_total / args.steps * 1e3 / max(1, 1), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "molecule": "benzene D6h (C r=2.6379, H r=4.68 bohr)", "basis": basis,
-                   "K": K, "parallelism": "replicas" if ws > 1 else "single", "l2": "flushed between steps (512 MB)",
-                   "launch_shape": shape},
+        "config": workload_config(K, ws),
+        "launch_shape": shape,
+        "served_stream": served,
+        "batched_scans": scans,
+        "mixed_precision": mixed,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-        "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val},
+        "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val, "reference_iterations": ref_iters},
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},
         "eri_rate": {"shell_quartets_per_s": s["quartets"] / (kernel_ms * 1e-3),
                      "primitive_quartets_per_s": s["prim_quartets"] / (kernel_ms * 1e-3),
                      "shell_quartets_per_build": s["quartets"], "note": "surviving (Schwarz-screened) quartets of one FP64 build"},
-        "mixed_precision": mixed,
-        "served_stream": served,
-        "batched_scans": scans,
         "roofline": {"bound": "fp64_pipe", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP64 FMA-loop peak of this GPU (hfx_measure_peaks, same run)",
-                     "flops_per_launch": flops, "kernel_ms": kernel_ms, "fp32_peak_tflops": fp32_peak / 1e3},
-        "e2e": {"value": whole_job_rate(1, e2e_t, ws), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                     "flops_per_launch": flops, "kernel_ms": kernel_ms, "fp32_peak_tflops": fp32_peak / 1e3,
+                     "dmma_peak_tflops": dmma_peak / 1e3 if dmma_peak else None},
+        "e2e": {"value": whole_job_rate(1, e2e_t, ws), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "solves": len(e2e_lat)},
         "gpu_launches": int(args.steps * builds * s["launches"]),
         "clocks": clk,
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    line["summary"] = summary(line)
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()
+
+
+def summary(line):
+    """Compact digest of the secondary sections, printed as the line's last key."""
+    out = {"roofline_frac_fp64": round(line["roofline"]["frac"], 4)}
+    mx = line.get("mixed_precision") or {}
+    if "speedup" in mx:
+        out["mixed"] = {k: (round(mx[k], 6) if isinstance(mx[k], float) else mx[k]) for k in
+                        ("speedup", "fp32_threshold", "fp32_quartet_fraction", "max_dF_vs_fp64", "scf_dE_vs_fp64",
+                         "fock_builds_per_s_fp64", "fock_builds_per_s_mixed")}
+        out["mixed"]["roofline_frac"] = round(mx["roofline"]["frac"], 4)
+    elif mx:
+        out["mixed"] = mx
+    sv = line.get("served_stream") or {}
+    if "rates" in sv:
+        rows = []
+        for e in sv["rates"]:
+            row = {"x": e["arrival_rate_x"]}
+            for key in ("one_at_a_time_fp64", "served_mixed", "served_mixed_packed"):
+                if key in e:
+                    row[key] = [round(e[key]["solves_per_s"], 3), round(e[key]["p99_s"], 2)]
+            rows.append(row)
+        out["served_solves_per_s_p99_s"] = rows
+    elif sv:
+        out["served"] = sv
+    sc = line.get("batched_scans") or {}
+    if "speedup" in sc:
+        out["scans"] = {"batched_solves_per_s": round(sc["batched"]["solves_per_s"], 3),
+                        "one_at_a_time_solves_per_s": round(sc["one_at_a_time_fp64"]["solves_per_s"], 3),
+                        "speedup": round(sc["speedup"], 3), "max_iteration_diff": sc["max_iteration_diff"]}
+    elif sc:
+        out["scans"] = sc
+    return out
 
 
 def section(fn, *a):
@@ -356,7 +428,7 @@ def section(fn, *a):
         return {"error": "%s: %s" % (type(e).__name__, e)}
 
 
-def mixed_section(H, W, torch, flush, args, local, scf_kw):
+def mixed_section(H, W, torch, flush, args, local, scf_kw, peaks):
     """n-decane/6-31G*: FP64 vs mixed Fock builds at the autotuned FP32 cut,
     max|dF| against the FP64 build, and the mixed SCF's |dE| against FP64."""
     cfg_d = W.n_decane()
@@ -371,17 +443,20 @@ def mixed_section(H, W, torch, flush, args, local, scf_kw):
     dPd = torch.tensor(Pd, device="cuda", dtype=torch.float64)
     dG64 = torch.zeros_like(dPd)
     dGmx = torch.zeros_like(dPd)
-    tms = {}
+    tms, kms = {}, {}
     for name, f, out in (("fp64", fb64, dG64), ("mixed", fbm, dGmx)):
         f.repulsion_matrix_device(dPd.data_ptr(), out.data_ptr())
-        ts = []
+        ts, ks = [], []
         for _ in range(max(3, args.steps)):
             flush_l2(torch, flush)
             torch.cuda.synchronize()
             f.repulsion_matrix_device(dPd.data_ptr(), out.data_ptr())
             ts.append(f.stats()["ms"])
+            ks.append(f.stats()["kernel_ms"])
         tms[name] = float(np.mean(ts))
+        kms[name] = float(np.mean(ks))
     smx = fbm.stats()
+    kms_mx = kms["mixed"]
     max_dF = float((dGmx - dG64).abs().max().item())
     rmx = H.rhf_diis(cfg_d, "6-31G*", precision=H.HFX_PREC_MIXED, fp32_threshold=tau, **scf_kw)
     mixed = {"workload": "n-decane C10H22 RHF/6-31G* (K=%d), seed 20261203 noise 0.05 bohr" % Kd,
@@ -392,7 +467,13 @@ def mixed_section(H, W, torch, flush, args, local, scf_kw):
              "max_dF_vs_fp64": max_dF, "scf_dE_vs_fp64": rmx["E_tot"] - r64["E_tot"],
              "scf_iterations_fp64": r64["iterations"], "scf_iterations_mixed": rmx["iterations"],
              "scf_fock_ms_fp64": r64["fock_ms"], "scf_fock_ms_mixed": rmx["fock_ms"],
-             "scf_builds_mixed_fp64_delta": [rmx["mixed_builds"], rmx["fp64_builds"], rmx["delta_builds"]]}
+             "scf_builds_mixed_fp64_delta": [rmx["mixed_builds"], rmx["fp64_builds"], rmx["delta_builds"]],
+             # pipe-time fraction of the mixed build's quartet kernels:
+             # (F64 / peak64 + F32 / peak32) / elapsed
+             "roofline": {"bound": "fp64+fp32 pipes", "flops_fp64": smx["flops_fp64"], "flops_fp32": smx["flops_fp32"],
+                          "kernel_ms": kms_mx, "peak_fp64_tflops": peaks[0] / 1e3, "peak_fp32_tflops": peaks[1] / 1e3,
+                          "frac": (smx["flops_fp64"] / (peaks[0] * 1e9) + smx["flops_fp32"] / (peaks[1] * 1e9))
+                          / (kms_mx * 1e-3)}}
     fbm.close()
     fb64.close()
     return mixed

@@ -25,7 +25,7 @@ from . import _lib
 from ._lib import BASIS_PATH, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError, check, lib, ptr
 
 __all__ = ["Basis", "basis_construction", "schwarz_bounds", "ERI_GPU", "FockBuilder", "rhf_diis", "uhf_diis",
-           "one_electron", "measure_peaks", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED", "BASIS_PATH",
+           "one_electron", "measure_peaks", "measure_dmma_peak", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED", "BASIS_PATH",
            "eri_index", "pair_index", "batch_scf"]
 
 
@@ -352,3 +352,10 @@ def measure_peaks(device=0):
     a, b = ctypes.c_double(), ctypes.c_double()
     check(lib.hfx_measure_peaks(device, ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+def measure_dmma_peak(device=0):
+    """FP64 tensor-core (mma.sync m8n8k4 f64) loop GFLOP/s of the device."""
+    a = ctypes.c_double()
+    check(lib.hfx_measure_dmma_peak(device, ctypes.byref(a)))
+    return a.value

@@ -151,6 +151,7 @@ SIGNATURES = {
     "hfx_points_eval": (I, [V, I, V, I, V, ctypes.c_longlong, V]),
     "hfx_last_error": (I, [ctypes.c_char_p, ctypes.c_size_t]),
     "hfx_measure_peaks": (I, [I, P(D), P(D)]),
+    "hfx_measure_dmma_peak": (I, [I, P(D)]),
     "hfx_server_create": (I, [V, P(V)]),
     "hfx_server_submit": (I, [V, V, P(ctypes.c_longlong)]),
     "hfx_server_poll": (I, [V, ctypes.c_longlong, V]),

@@ -33,4 +33,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python import_basis.py <reference checkout root>")
+    main(sys.argv[1])

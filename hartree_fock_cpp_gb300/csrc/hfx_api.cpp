@@ -27,6 +27,7 @@ namespace hfx {
 // in the mixed-precision SCF (Q_AB Q_CD max|dD| below this: quartet skipped)
 constexpr double kDeltaThr = 1e-12;
 void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG);   // hfx_noalloc.cu
+void noalloc_prepare(int device);                                            // hfx_noalloc.cu
 void grid_eval(const Basis& b, int device, const double* M, int column, const double* xyz, long long n, int res,
                const double* start, const double* step, double* out);                  // hfx_grid.cu
 static thread_local std::string g_last_error;
@@ -81,6 +82,7 @@ hfx_status hfx_create(const hfx_functions* basis, const hfx_options* opt, hfx_jo
         *job = nullptr;
         auto j = std::make_unique<hfx_job>();
         j->job = std::make_unique<Job>(basis_from_functions(*basis), default_options(opt));
+        noalloc_prepare(j->job->device());
         *job = j.release();
     });
 }
@@ -92,6 +94,7 @@ hfx_status hfx_create_molecule(const hfx_molecule* mol, const hfx_options* opt, 
         *job = nullptr;
         auto j = std::make_unique<hfx_job>();
         j->job = std::make_unique<Job>(build_basis(*mol), default_options(opt));
+        noalloc_prepare(j->job->device());
         *job = j.release();
     });
 }

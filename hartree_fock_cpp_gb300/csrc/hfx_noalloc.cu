@@ -15,8 +15,9 @@
 // Limits: K <= kNoAllocMaxK basis functions and at most kNoAllocMaxGroups
 // kernel launch groups per build; larger jobs are rejected with
 // HFX_ERR_UNSUPPORTED.  The array (2 * 512 * 512 doubles + 64 ints, about
-// 4 MB) is reserved on every device that loads the library, until the
-// process exits.  All calls share it: two builds that overlap on the GPU (two
+// 4 MB) is reserved on a device when the first job is created there (module
+// loading is lazy by default; job creation resolves the array's address) and
+// stays reserved until the process exits.  All calls share it: two builds that overlap on the GPU (two
 // host threads, or two jobs on different streams) race on it and produce
 // garbage, so callers serialise them.  Each call clears the parts that must
 // start at zero.
@@ -59,6 +60,12 @@ static NoAllocScratch* scratch_address(int device)
     }
     return addr[device];
 }
+
+// Job creation resolves the address on the job's device, so that the first
+// allocation-free build makes no CUDA call that could allocate: with lazy
+// module loading (the CUDA default), resolving the symbol loads the module
+// that holds the array, which reserves its memory.
+void noalloc_prepare(int device) { scratch_address(device); }
 
 void fock_rhf_noalloc(Job& job, int device, const double* dP, double* dG)
 {

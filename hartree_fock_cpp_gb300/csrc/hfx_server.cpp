@@ -253,8 +253,7 @@ private:
                     std::vector<std::shared_ptr<ServerJob>> pack{j};
                     for (auto it = queue_.begin(); it != queue_.end() && (int)pack.size() < opt_.pack_max;) {
                         auto& c = *it;
-                        if (!c->cancel && c->method == j->method && c->precision == j->precision &&
-                            c->fp32_threshold == j->fp32_threshold) {
+                        if (!c->cancel && same_job_options(*c, *j)) {
                             c->state = HFX_JOB_RUNNING;
                             c->t_admit = now_s();
                             ++running_;
@@ -283,6 +282,40 @@ private:
             done_cv_.notify_all();
             cv_.notify_all();
         }
+    }
+
+    // Requests that may share one packed job: the same method and the same job
+    // options (every field of hfx_options the packed job is built with), so
+    // that each member is computed exactly as it would be alone.
+    static bool same_job_options(const ServerJob& a, const ServerJob& b)
+    {
+        return a.method == b.method && a.precision == b.precision && a.fp32_threshold == b.fp32_threshold &&
+               a.scf.screening_threshold == b.scf.screening_threshold;
+    }
+
+    // Reserve without waiting: false when the footprint does not fit now.
+    bool try_reserve(ServerJob& j, size_t bytes)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (bytes > budget_) throw Error(HFX_ERR_OOM, "estimated device footprint exceeds the server's HBM budget");
+        if (in_use_ + bytes > budget_) return false;
+        in_use_ += bytes;
+        j.footprint = bytes;
+        return true;
+    }
+
+    // A pack member that must wait for memory goes back to the head of the
+    // queue instead: the memory it waits for may be held by its own pack.
+    void requeue(const std::shared_ptr<ServerJob>& j)
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            j->state = HFX_JOB_QUEUED;
+            j->t_admit = 0.0;
+            --running_;
+            queue_.push_front(j);
+        }
+        cv_.notify_one();
     }
 
     // reserve the job's footprint, waiting (bounded by the job's timeout) for
@@ -347,7 +380,12 @@ private:
                 j->K = b.K;
                 size_t fp = estimate_footprint(b);
                 if (j->inject_fault == HFX_FAULT_OOM) fp = budget_ + 1;
-                reserve(*j, fp);
+                if (live.empty()) {
+                    reserve(*j, fp);
+                } else if (!try_reserve(*j, fp)) {
+                    requeue(j);
+                    continue;
+                }
                 if (j->inject_fault == HFX_FAULT_ALLOC) throw Error(HFX_ERR_OOM, "injected allocation failure");
                 bases.push_back(std::move(b));
                 live.push_back(j);

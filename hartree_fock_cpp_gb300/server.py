@@ -31,7 +31,7 @@ class Server:
 
     def submit(self, config, basis_set, method="RHF", spin=None, charge=0, epsilon=1e-6, energy_threshold=0.0,
                max_it=10000, precision=-1, fp32_threshold=0.0, timeout_s=0.0, inject_fault="none",
-               basis_path=None):
+               basis_path=None, screening_threshold=1e-8):
         m = _lib.MoleculeArgs(config, basis_set, basis_path)
         r = _lib.Request()
         r.mol = m.c
@@ -42,7 +42,7 @@ class Server:
         r.scf.epsilon = epsilon
         r.scf.energy_threshold = energy_threshold
         r.scf.charge = charge
-        r.scf.screening_threshold = 1e-8
+        r.scf.screening_threshold = screening_threshold
         r.precision = precision
         r.fp32_threshold = fp32_threshold
         r.timeout_s = timeout_s

@@ -133,9 +133,10 @@ hfx_status hfx_fock_uhf_device(hfx_job *job, const double *dPa, const double *dP
  * owns the GPU memory, or a loop that must not let cudaMalloc synchronise
  * the device).  No counterpart in the reference.  It allocates nothing: its
  * scratch (J/K accumulators, work-queue counters) lives in one static device
- * array of about 4 MB, reserved on every device that loads the library.
- * Limits: K <= 512, else HFX_ERR_UNSUPPORTED.  The first call on a device
- * resolves that array's address; make it before any stream capture.  All
+ * array of about 4 MB, reserved on a device when the first job is created
+ * there (job creation resolves the array's address, which under CUDA's
+ * default lazy module loading loads the module holding it) and kept until the
+ * process exits.  Limits: K <= 512, else HFX_ERR_UNSUPPORTED.  All
  * calls share the array, so calls that overlap on the GPU race; serialise
  * them.  The job itself must already exist (hfx_create allocates). */
 hfx_status hfx_fock_rhf_device_noalloc(hfx_job *job, const double *dP, double *dG);
@@ -407,6 +408,10 @@ hfx_status hfx_last_error(char *buf, size_t n);
 
 /* FP64 / FP32 FMA-loop peak of the device, GFLOP/s (roofline denominators). */
 hfx_status hfx_measure_peaks(int device, double *fp64_gflops, double *fp32_gflops);
+/* FP64 tensor-core (DMMA: mma.sync m8n8k4 f64) loop throughput, GFLOP/s:
+ * the ceiling of a tensor-core Hermite->Cartesian transform.  No counterpart
+ * in the reference (its transforms are scalar FP64, cuda/include/kernels.cuh:6-80). */
+hfx_status hfx_measure_dmma_peak(int device, double *gflops);
 
 #ifdef __cplusplus
 }

@@ -497,3 +497,102 @@ void orc_exchange_matrix(int K, const double *P, const double *eri, double *Kx)
             Kx[i * K + j] = s;
         }
 }
+
+/* ---------------- threaded drivers (fixture generation) -----------------
+ * The reference is single-threaded; these only spread its loops over host
+ * threads.  Every output element is computed by exactly the code above, in
+ * the same order, so the results are bit-identical to the serial functions. */
+
+typedef struct {
+    const orc_basis *bs;
+    const double *bounds;
+    double thr;
+    double *out;
+    size_t nq;
+    size_t *next;          /* shared block counter */
+    int K;
+    const double *P1, *P2, *eri;
+    int kind;              /* 0 tensor, 1 repulsion, 2 coulomb, 3 exchange, 4 schwarz */
+    size_t block;          /* items per claimed task */
+} mt_job;
+
+static void *mt_worker(void *arg)
+{
+    mt_job *j = (mt_job *)arg;
+    for (;;) {
+        size_t b = __atomic_fetch_add(j->next, j->block, __ATOMIC_RELAXED);
+        if (b >= j->nq) break;
+        size_t e = b + j->block < j->nq ? b + j->block : j->nq;
+        if (j->kind == 0) {
+            orc_repulsion_tensor_range(j->bs, j->bounds, j->thr, j->out, b, e);
+        } else if (j->kind == 4) {
+            for (size_t p = b; p < e; ++p) {
+                int a, c;
+                pair_to_indices((int)p, &a, &c);
+                double v = orc_basis_repulsion(j->bs, a, c, a, c);
+                j->out[p] = sqrt(v > 0.0 ? v : 0.0);
+            }
+        } else {
+            int K = j->K;
+            for (size_t r = b; r < e; ++r) {           /* r = i*K + j, one output element */
+                int i = (int)(r / K), jj = (int)(r % K);
+                double s = 0.0;
+                for (int k = 0; k < K; ++k)
+                    for (int l = 0; l < K; ++l) {
+                        if (j->kind == 1) {
+                            double Jv = j->P1[k * K + l] * j->eri[orc_eri_index(i, jj, k, l)];
+                            double Kv = j->P1[k * K + l] * j->eri[orc_eri_index(i, k, jj, l)];
+                            s += Jv - 0.5 * Kv;
+                        } else if (j->kind == 2) {
+                            s += (j->P1[k * K + l] + j->P2[k * K + l]) * j->eri[orc_eri_index(i, jj, k, l)];
+                        } else {
+                            s += j->P1[k * K + l] * j->eri[orc_eri_index(i, k, jj, l)];
+                        }
+                    }
+                j->out[r] = s;
+            }
+        }
+    }
+    return NULL;
+}
+
+static void mt_run(mt_job *proto, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    size_t next = 0;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    mt_job *jobs = (mt_job *)malloc(sizeof(mt_job) * nthreads);
+    for (int t = 0; t < nthreads; ++t) {
+        jobs[t] = *proto;
+        jobs[t].next = &next;
+        pthread_create(&th[t], NULL, mt_worker, &jobs[t]);
+    }
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    free(th);
+    free(jobs);
+}
+
+/* schwarz_bounds + repulsion_tensor (integrals.hpp:732-787) over nthreads */
+void orc_repulsion_tensor_mt(const orc_basis *bs, double threshold, double *out, int nthreads)
+{
+    size_t n_pairs = (size_t)bs->K * (bs->K + 1) / 2;
+    double *bounds = (double *)malloc(n_pairs * sizeof(double));
+    mt_job j;
+    memset(&j, 0, sizeof j);
+    j.bs = bs; j.out = bounds; j.nq = n_pairs; j.kind = 4; j.block = 8;
+    mt_run(&j, nthreads);
+    memset(&j, 0, sizeof j);
+    j.bs = bs; j.bounds = bounds; j.thr = threshold; j.out = out; j.nq = n_pairs * (n_pairs + 1) / 2; j.kind = 0; j.block = 1024;
+    mt_run(&j, nthreads);
+    free(bounds);
+}
+
+/* linalg.hpp:100-129 / 215-257 / 260-296 over nthreads (one output element per task) */
+void orc_contract_mt(int kind, int K, const double *P1, const double *P2, const double *eri, double *out,
+                     int nthreads)
+{
+    mt_job j;
+    memset(&j, 0, sizeof j);
+    j.K = K; j.P1 = P1; j.P2 = P2; j.eri = eri; j.out = out; j.nq = (size_t)K * K; j.kind = kind; j.block = 4;
+    mt_run(&j, nthreads);
+}

@@ -126,11 +126,21 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def reference_checkout():
+    """Directory of a reference checkout, from the HF_REFERENCE environment
+    variable; None when it is unset or does not hold the reference."""
+    ref = os.environ.get("HF_REFERENCE")
+    if ref and os.path.isdir(os.path.join(ref, "include")):
+        return ref
+    return None
+
+
 def build_oracle():
-    """Compile hf_oracle.c (and the reference shim where the reference exists)."""
+    """Compile hf_oracle.c (and the reference shim where a checkout is given)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if os.path.isdir("/root/reference/include"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    ref = reference_checkout()
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True)
 
 
 _lib = None
@@ -162,6 +172,9 @@ def lib():
         L.orc_attraction.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p]
         L.orc_repulsion_matrix.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_repulsion_tensor_mt.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
+        L.orc_contract_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.orc_coulomb_matrix.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p]
         L.orc_exchange_matrix.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -199,6 +212,14 @@ class Oracle:
         npair = self.K * (self.K + 1) // 2
         out = np.zeros(npair * (npair + 1) // 2)
         lib().orc_repulsion_tensor(ctypes.byref(self._c), threshold, _ptr(out))
+        return out
+
+    def repulsion_tensor_mt(self, threshold=1e-8, nthreads=None):
+        """repulsion_tensor spread over host threads (bit-identical result)."""
+        self._mode()
+        npair = self.K * (self.K + 1) // 2
+        out = np.zeros(npair * (npair + 1) // 2)
+        lib().orc_repulsion_tensor_mt(ctypes.byref(self._c), threshold, _ptr(out), nthreads or os.cpu_count())
         return out
 
     def eri_list(self, ijkl, bounds=None, threshold=1e-8, nthreads=1):
@@ -293,6 +314,19 @@ def exchange_matrix(P, eri):                # linalg.hpp:260-296
     Kx = np.zeros((K, K))
     lib().orc_exchange_matrix(K, _ptr(P), _ptr(eri), _ptr(Kx))
     return Kx
+
+
+def contract_mt(kind, P1, eri, P2=None, nthreads=None):
+    """repulsion_matrix ("G"), coulomb_matrix ("J", P1 + P2) or
+    exchange_matrix ("K") spread over host threads; each element is the
+    serial function's sum in the same order."""
+    K = P1.shape[0]
+    P1 = np.ascontiguousarray(P1, dtype=np.float64)
+    P2 = np.ascontiguousarray(P2 if P2 is not None else np.zeros((K, K)), dtype=np.float64)
+    out = np.zeros((K, K))
+    lib().orc_contract_mt({"G": 1, "J": 2, "K": 3}[kind], K, _ptr(P1), _ptr(P2), _ptr(eri), _ptr(out),
+                          nthreads or os.cpu_count())
+    return out
 
 
 def eri_index(i, j, k, l):                  # indexing.hpp:42-53
@@ -539,6 +573,7 @@ class RefLib:
         L.ref_basis_repulsion.argtypes = [ctypes.c_int] * 4
         L.ref_schwarz_bounds.argtypes = [ctypes.c_void_p]
         L.ref_repulsion_tensor.argtypes = [ctypes.c_double, ctypes.c_void_p]
+        L.ref_repulsion_tensor_mt.argtypes = [ctypes.c_double, ctypes.c_void_p, ctypes.c_int]
         L.ref_one_electron.argtypes = [ctypes.c_void_p] * 3
         L.ref_nprims_total.restype = ctypes.c_int
         L.ref_export_basis.argtypes = [ctypes.c_void_p] * 6
@@ -571,6 +606,12 @@ class RefLib:
         npair = self.K * (self.K + 1) // 2
         out = np.zeros(npair * (npair + 1) // 2)
         self.L.ref_repulsion_tensor(threshold, _ptr(out))
+        return out
+
+    def repulsion_tensor_mt(self, threshold=1e-8, nthreads=None):
+        npair = self.K * (self.K + 1) // 2
+        out = np.zeros(npair * (npair + 1) // 2)
+        self.L.ref_repulsion_tensor_mt(threshold, _ptr(out), nthreads or os.cpu_count())
         return out
 
     def eri(self, i, j, k, l):

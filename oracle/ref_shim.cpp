@@ -6,7 +6,9 @@
 // to pin the C restatement (hf_oracle.c) and to generate the golden fixtures
 // under tests/golden/.  Nothing in the engine links it.
 #include "integrals.hpp"   // brings basis.hpp, atoms.hpp, types.hpp, indexing.hpp
+#include <atomic>
 #include <cstring>
+#include <thread>
 
 static std::vector<basis_function> g_basis;
 static std::vector<atom> g_atoms;
@@ -67,6 +69,48 @@ void ref_repulsion_tensor(double threshold, double* out)
 {
     auto e = repulsion_tensor(g_basis, threshold);
     std::memcpy(out, e.data(), e.size() * sizeof(double));
+}
+
+// repulsion_tensor (integrals.hpp:754-787) with its Schwarz pass and quartet
+// loop spread over nthreads host threads (harness only: each element is still
+// one call of the reference's basis_repulsion, with the reference's own
+// schwarz test and index helpers, so the array equals repulsion_tensor's).
+void ref_repulsion_tensor_mt(double threshold, double* out, int nthreads)
+{
+    if (nthreads < 1) nthreads = 1;
+    const int K = (int)g_basis.size();
+    const size_t n_pairs = (size_t)K * (K + 1) / 2;
+    const size_t n_quartets = n_pairs * (n_pairs + 1) / 2;
+    std::vector<double> bounds(n_pairs);
+    auto par = [&](size_t n, size_t block, auto body) {
+        std::atomic<size_t> next{0};
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthreads; ++t)
+            th.emplace_back([&] {
+                for (;;) {
+                    size_t b = next.fetch_add(block);
+                    if (b >= n) break;
+                    size_t e = std::min(n, b + block);
+                    for (size_t i = b; i < e; ++i) body(i);
+                }
+            });
+        for (auto& t : th) t.join();
+    };
+    par(n_pairs, 8, [&](size_t i) {
+        std::pair<int, int> idx = pair_to_indices((int)i);
+        double b = basis_repulsion(g_basis[idx.first], g_basis[idx.second], g_basis[idx.first], g_basis[idx.second]);
+        bounds[i] = std::sqrt(std::max(b, 0.0));
+    });
+    par(n_quartets, 1024, [&](size_t i) {
+        std::pair<int, int> q = quartet_to_pairs(i);
+        std::pair<int, int> p1 = pair_to_indices(q.first);
+        std::pair<int, int> p2 = pair_to_indices(q.second);
+        if (bounds[q.first] * bounds[q.second] < threshold) {
+            out[i] = 0.0;
+            return;
+        }
+        out[i] = basis_repulsion(g_basis[p1.first], g_basis[p1.second], g_basis[p2.first], g_basis[p2.second]);
+    });
 }
 
 void ref_one_electron(double* S, double* T, double* V)

@@ -6,7 +6,8 @@ Sources (read here only; nothing at test time reads the reference):
     Schwarz bounds and one-electron matrices;
   * the reference's published SCF results results/STO-3G/*_vr.csv (R, E
     curves of its own RHF code): a few points per curve.
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:
+  HF_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 """
 import csv
 import json
@@ -21,7 +22,7 @@ sys.path.insert(0, REPO)
 import oracle as O  # noqa: E402
 from hartree_fock_cpp_gb300 import workloads as W  # noqa: E402
 
-REF = os.environ.get("HF_REFERENCE", "/root/reference")
+REF = O.reference_checkout()     # HF_REFERENCE: a checkout of the reference
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -93,6 +94,8 @@ def energies():
 
 
 def main():
+    if REF is None:
+        sys.exit("set HF_REFERENCE to a checkout of the reference")
     O.build_oracle()
     json.dump(water_sto3g(), open(os.path.join(OUT, "water_sto3g.json"), "w"))
     samples = [eri_samples("water_631gs", W.water(), "6-31G*"),

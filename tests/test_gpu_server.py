@@ -97,3 +97,32 @@ def test_packed_mode_results_same_alone_and_in_the_pack():
         assert abs(inf["iterations"] - a["iterations"]) <= 1
     assert ib["state"] == "failed"
     assert iu["state"] == "done" and iu["converged"]
+
+
+def test_packed_members_keep_their_own_screening_threshold():
+    """Requests with different Schwarz thresholds never share a packed job:
+    each result equals the same request run alone."""
+    thr = (1e-8, 1e-3)
+    alone = [H.rhf_diis(W.water(), "cc-pVDZ", screening_threshold=t) for t in thr]
+    assert abs(alone[0]["E_tot"] - alone[1]["E_tot"]) > 10 * E_TOL   # the thresholds matter
+    with Server(max_active=1, pack_max=4) as srv:
+        ids = [srv.submit(W.water(), "cc-pVDZ", screening_threshold=t) for t in thr]
+        srv.drain(300)
+        infos = [srv.poll(i) for i in ids]
+    for a, inf in zip(alone, infos):
+        assert inf["state"] == "done" and inf["converged"], inf
+        assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL
+
+
+def test_packed_admission_never_waits_on_its_own_pack():
+    """The budget fits one request but not two: the pack runs the member that
+    fits and requeues the others instead of waiting for memory that only the
+    pack itself would release."""
+    with Server(max_active=1, pack_max=4, hbm_budget_gb=0.1) as srv:
+        ids = [srv.submit(W.water(), "STO-3G") for _ in range(3)]
+        srv.drain(120)
+        infos = [srv.poll(i) for i in ids]
+        st = srv.stats()
+    for inf in infos:
+        assert inf["state"] == "done" and inf["converged"], inf
+    assert st["in_use_bytes"] == 0
