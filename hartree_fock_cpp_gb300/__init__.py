@@ -188,6 +188,17 @@ class FockBuilder:
         return dict(small_chunk=s.small_chunk, warp_chunk=s.warp_chunk, warp_max_warps=s.warp_max_warps,
                     lane_min_npp=s.lane_min_npp), ms.value
 
+    def plan(self, mixed=None):
+        """Launch groups of the job's Fock-build plan (the mixed plan of a mixed
+        job unless mixed=False): one dict per group."""
+        m = 1 if mixed is None or mixed else 0
+        n = ctypes.c_int()
+        check(lib.hfx_debug_plan(self._job, m, ctypes.byref(n), None))
+        rows = np.zeros((n.value, 10))
+        check(lib.hfx_debug_plan(self._job, m, ctypes.byref(n), ptr(rows)))
+        keys = ("kind", "pcb", "pck", "fp32", "tasks", "flops", "prims", "grid", "slice", "warps_per_cta")
+        return [{k: (float(v) if k in ("flops", "prims") else int(v)) for k, v in zip(keys, r)} for r in rows]
+
     def stats(self):
         s = _lib.BuildStats()
         check(lib.hfx_last_build_stats(self._job, ctypes.byref(s)))
@@ -291,12 +302,15 @@ def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_
 
 def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsilon=1e-6, damping=0.3,
               screening_threshold=1e-8, energy_threshold=0.0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
-              max_parallel=0, param_path=None):
+              max_parallel=0, param_path=None, warm_chain=0):
     """Lockstep batched SCF (hfx_batch_scf): `molecules` is a list of
     (config, basis_set); all of them iterate together on one packed job, one
     Fock build per SCF cycle over every molecule still iterating.  The
     batched counterpart of the reference's sequential scan drivers
-    (run.hpp:300-423, 498-577); every molecule starts from the zero density.
+    (run.hpp:300-423, 498-577).  warm_chain = c > 1: chains of c consecutive
+    molecules, each starting from the previous one's final density (the
+    reference scan's warm start, run.hpp:353-368), the chains iterating
+    together; otherwise every molecule starts from the zero density.
     UHF takes spins = [(n_alpha, n_beta), ...].  Returns (results, stats):
     one dict per molecule (E_tot, iterations, converged, ...) and the batch's
     timing."""
@@ -317,6 +331,7 @@ def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsil
     bo = _lib.BatchOptions()
     bo.method = 1 if uhf else 0
     bo.max_parallel = int(max_parallel)
+    bo.warm_chain = int(warm_chain)
     res = (_lib.ScfResult * n)()
     st = _lib.BatchStats()
     status = lib.hfx_batch_scf(ctypes.cast(mols, ctypes.c_void_p), n, ptr(na), ptr(nb), ctypes.byref(o),

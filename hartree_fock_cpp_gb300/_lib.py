@@ -95,7 +95,8 @@ class ServerStats(ctypes.Structure):
 
 
 class BatchOptions(ctypes.Structure):
-    _fields_ = [("method", ctypes.c_int), ("max_parallel", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+    _fields_ = [("method", ctypes.c_int), ("max_parallel", ctypes.c_int), ("warm_chain", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
 
 
 class BatchStats(ctypes.Structure):
@@ -144,6 +145,7 @@ SIGNATURES = {
     "hfx_build_functions": (I, [V, P(I), P(I), V, V, V, V, V, V]),
     "hfx_debug_pair_data": (I, [V, P(I), P(I), P(ctypes.c_longlong), V, V, V]),
     "hfx_debug_packed_pairs": (I, [V, I, P(I), V, V]),
+    "hfx_debug_plan": (I, [V, I, P(I), V]),
     "hfx_one_electron": (I, [V, V, V, V, P(I)]),
     "hfx_one_electron_gpu": (I, [V, I, V, V, V, P(I)]),
     "hfx_grid_density": (I, [V, I, V, V, D, I, V]),

@@ -1,7 +1,7 @@
 """The reference's JSON-driven apps on the GPU engine:
 
   python -m hartree_fock_cpp_gb300.apps single_run   input.json
-  python -m hartree_fock_cpp_gb300.apps bl_scan      input.json [--batched]
+  python -m hartree_fock_cpp_gb300.apps bl_scan      input.json [--batched [--warm-chain N]]
   python -m hartree_fock_cpp_gb300.apps dissociation input.json
 
 Input keys, defaults and validation follow include/run.hpp (read_scf_options
@@ -13,9 +13,10 @@ plain K x K tables.
 
 eri_hardware "GPU" runs the engine; "CPU" names the reference's own
 stored-tensor path, which this library does not contain, and is rejected.
-bl_scan --batched solves every scan geometry at once on one packed job
-(batch_scf: one Fock build per SCF cycle over all points still iterating,
-cold-start densities); without it the scan runs point after point with the
+bl_scan --batched solves the scan geometries together on one packed job
+(batch_scf: one Fock build per SCF cycle over all points still iterating), in
+chains of --warm-chain consecutive points that start from the previous
+point's density; without it the scan runs point after point with the
 previous density as the initial guess, as run_bl_scan does
 (run.hpp:329-368).  dissociation solves the free atoms as one UHF batch.
 """
@@ -180,11 +181,13 @@ def scan_geometry(opt, r):
     return cfg
 
 
-def run_bl_scan(opt, batched=False, max_parallel=0):
-    """run.hpp:300-423.  batched=True solves every point at once on one packed
-    job (batch_scf: one Fock build per SCF cycle over all points still
-    iterating, each point from the zero density) instead of one after the
-    other with warm starts; homo/lumo are then not reported (NaN)."""
+def run_bl_scan(opt, batched=False, max_parallel=0, warm_chain=8):
+    """run.hpp:300-423.  batched=True solves the points together on one
+    packed job (batch_scf: one Fock build per SCF cycle over all points still
+    iterating) in chains of warm_chain consecutive points, each point of a
+    chain starting from the previous point's density as in the sequential
+    scan (warm_chain <= 1: every point from the zero density); homo/lumo are
+    then not reported (NaN)."""
     t0 = time.time()
     dist = scan_distances(opt["distances"])
     E, homo, lumo, its = [], [], [], []
@@ -193,7 +196,7 @@ def run_bl_scan(opt, batched=False, max_parallel=0):
         kw = _scf_kw(opt)
         kw.pop("eri_device")
         res, _ = batch_scf([(scan_geometry(opt, r), opt["basis"]) for r in dist], max_parallel=max_parallel,
-                           param_path=opt["basis_path"], **kw)
+                           param_path=opt["basis_path"], warm_chain=warm_chain, **kw)
         for r in res:
             E.append(r["E_tot"])
             its.append(r["iterations"])
@@ -259,13 +262,15 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m hartree_fock_cpp_gb300.apps")
     ap.add_argument("app", choices=["single_run", "bl_scan", "dissociation"])
     ap.add_argument("input")
-    ap.add_argument("--batched", action="store_true", help="bl_scan: all points at once on one packed job")
+    ap.add_argument("--batched", action="store_true", help="bl_scan: the points together on one packed job")
+    ap.add_argument("--warm-chain", type=int, default=8,
+                    help="bl_scan --batched: consecutive points per warm-started chain (<= 1: all cold)")
     a = ap.parse_args(argv)
     if a.app == "single_run":
         r = run_scf_from_options(read_scf_options(a.input))
         print("E_tot = %.10f  iterations = %d  converged = %s" % (r["E_tot"], r["iterations"], r["converged"]))
     elif a.app == "bl_scan":
-        r = run_bl_scan(read_blscan_options(a.input), batched=a.batched)
+        r = run_bl_scan(read_blscan_options(a.input), batched=a.batched, warm_chain=a.warm_chain)
         for d, e in zip(r["distances"], r["energies"]):
             print("%.6f %.10f" % (d, e))
     else:

@@ -508,6 +508,22 @@ hfx_status hfx_debug_packed_pairs(const hfx_molecule* mols, int n, int* npairs, 
     });
 }
 
+hfx_status hfx_debug_plan(const hfx_job* job, int mixed, int* ngroups, double* rows)
+{
+    return guarded([&] {
+        if (!job || !ngroups) throw Error(HFX_ERR_INVALID, "null argument");
+        const auto& groups = job->job->plan_groups(mixed != 0);
+        *ngroups = (int)groups.size();
+        if (!rows) return;
+        for (size_t g = 0; g < groups.size(); ++g) {
+            const LaunchGroup& x = groups[g];
+            double* r = rows + 10 * g;
+            r[0] = x.kind; r[1] = x.pcb; r[2] = x.pck; r[3] = x.fp32 ? 1 : 0; r[4] = (double)x.n;
+            r[5] = x.flops; r[6] = x.prims; r[7] = x.grid; r[8] = x.slice; r[9] = x.warps_per_cta;
+        }
+    });
+}
+
 hfx_status hfx_one_electron(const hfx_molecule* mol, double* S, double* T, double* V, int* K)
 {
     return guarded([&] {

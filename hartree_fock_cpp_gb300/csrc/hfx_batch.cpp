@@ -240,32 +240,55 @@ PackedRunStats run_packed(const std::vector<Basis>& bases, const hfx_options& jo
     Job job(bases, jo);
     PackedBuilder builder(job, nspin);
     const double t_setup = now_s() - t0;
-    const int workers = std::max(1, std::min({n, max_parallel > 0 ? max_parallel : n, 256}));
+    // chains of consecutive molecules linked by warm_from (a molecule with
+    // warm_from == -1 starts a new chain)
+    std::vector<std::vector<int>> chains;
+    for (int i = 0; i < n; ++i) {
+        if (members[i].warm_from >= 0 && members[i].warm_from != i - 1)
+            throw Error(HFX_ERR_INVALID, "packed run: a molecule can only start from the preceding one's density");
+        if (members[i].warm_from < 0 || chains.empty()) chains.emplace_back();
+        chains.back().push_back(i);
+    }
+    const int nchains = (int)chains.size();
+    const int workers = std::max(1, std::min({nchains, max_parallel > 0 ? max_parallel : nchains, 256}));
     std::atomic<int> next{0};
     int dev = 0;
     cudaGetDevice(&dev);
     auto worker = [&] {
         cudaSetDevice(dev);
-        for (int i = next++; i < n; i = next++) {
-            bool joined = false;
-            try {
-                const PackedMember& m = members[i];
-                ScfSetup setup = scf_setup(bases[i], true);
-                BatchMember member(builder, i, bases[i].K, job.mixed());
-                DeviceScf d(member, setup, nspin);
-                builder.join();
-                joined = true;
-                ScfOutput out = d.run(bases[i], setup, m.scf, m.n_alpha, m.n_beta, nullptr, nullptr, kBatchDeltaThr,
-                                      m.ctl);
-                builder.leave();
-                joined = false;
-                done(i, &out, out.converged ? HFX_OK : HFX_ERR_NOT_CONVERGED, std::string());
-            } catch (const Error& e) {
-                if (joined) builder.leave();
-                done(i, nullptr, e.code, e.what());
-            } catch (const std::exception& e) {
-                if (joined) builder.leave();
-                done(i, nullptr, HFX_ERR_CUDA, e.what());
+        for (int c = next++; c < nchains; c = next++) {
+            std::vector<double> prevA, prevB;   // final densities of the chain's previous molecule
+            for (int i : chains[c]) {
+                bool joined = false;
+                // warm start only from a density of this molecule's size
+                const bool warm = members[i].warm_from >= 0 && !prevA.empty() &&
+                                  prevA.size() == (size_t)bases[i].K * bases[i].K &&
+                                  (nspin == 1 || prevB.size() == prevA.size());
+                try {
+                    const PackedMember& m = members[i];
+                    ScfSetup setup = scf_setup(bases[i], true);
+                    BatchMember member(builder, i, bases[i].K, job.mixed());
+                    DeviceScf d(member, setup, nspin);
+                    builder.join();
+                    joined = true;
+                    ScfOutput out = d.run(bases[i], setup, m.scf, m.n_alpha, m.n_beta, warm ? prevA.data() : nullptr,
+                                          warm && nspin == 2 ? prevB.data() : nullptr, kBatchDeltaThr, m.ctl);
+                    builder.leave();
+                    joined = false;
+                    prevA = out.P;
+                    prevB = out.P2;
+                    done(i, &out, out.converged ? HFX_OK : HFX_ERR_NOT_CONVERGED, std::string());
+                } catch (const Error& e) {
+                    if (joined) builder.leave();
+                    prevA.clear();
+                    prevB.clear();
+                    done(i, nullptr, e.code, e.what());
+                } catch (const std::exception& e) {
+                    if (joined) builder.leave();
+                    prevA.clear();
+                    prevB.clear();
+                    done(i, nullptr, HFX_ERR_CUDA, e.what());
+                }
             }
         }
     };
@@ -307,10 +330,12 @@ extern "C" hfx_status hfx_batch_scf(const hfx_molecule* mols, int n, const int* 
         jo.precision = o.precision;
         jo.fp32_threshold = o.fp32_threshold;
         std::vector<PackedMember> members(n);
+        if (b.warm_chain < 0) throw Error(HFX_ERR_INVALID, "batch: warm_chain must be >= 0");
         for (int i = 0; i < n; ++i) {
             members[i].scf = o;
             members[i].n_alpha = nspin == 2 ? n_alpha[i] : 0;
             members[i].n_beta = nspin == 2 ? n_beta[i] : 0;
+            members[i].warm_from = (b.warm_chain > 1 && i % b.warm_chain != 0) ? i - 1 : -1;
         }
         std::vector<hfx_status> status(n, HFX_OK);
         std::vector<std::string> msg(n);

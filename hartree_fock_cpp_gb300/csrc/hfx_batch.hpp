@@ -16,6 +16,11 @@ struct PackedMember {
     hfx_scf_options scf{};
     int n_alpha = 0, n_beta = 0;    // UHF occupations
     const ScfControl* ctl = nullptr;
+    // index of the molecule whose final density this one starts from (the
+    // reference's scan warm start, run.hpp:353-368), or -1 for the zero
+    // density; only the directly preceding molecule (index - 1) is allowed,
+    // so that warm-started molecules form chains solved one after another
+    int warm_from = -1;
 };
 
 struct PackedRunStats {
@@ -31,8 +36,10 @@ struct PackedRunStats {
 using PackedDone = std::function<void(int index, ScfOutput* out, hfx_status status, const std::string& message)>;
 
 // Runs the SCFs of `bases` (one method: nspin 1 = RHF, 2 = UHF) in lockstep
-// on one packed job built with options jo; at most max_parallel molecules
-// iterate at once (0: all, capped at 256).  Throws only when the packed job
+// on one packed job built with options jo.  Molecules linked by warm_from
+// form chains (a chain's molecules run one after another, each from the
+// previous one's final density); at most max_parallel chains iterate at once
+// (0: all, capped at 256).  Throws only when the packed job
 // itself cannot be built; every molecule's own failure goes to done.
 PackedRunStats run_packed(const std::vector<Basis>& bases, const hfx_options& jo, int nspin,
                           const std::vector<PackedMember>& members, int max_parallel, const PackedDone& done);

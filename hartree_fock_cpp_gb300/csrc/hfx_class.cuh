@@ -189,12 +189,12 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
 
     const T* __restrict__ recb = a.rec + bra.rec_off;
     const T* __restrict__ reck = a.rec + ket.rec_off;
-    const int ij1 = tk.ij >> 16;
-    for (int ij = tk.ij & 0xffff; ij < ij1; ++ij) {
+    const int ij1 = tk.i1, kl0 = tk.k0, kl1 = tk.k1;
+    for (int ij = tk.i0; ij < ij1; ++ij) {
         const T* rb = recb + ij * SB;
         const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
         const T* cb = rb + 5;
-        for (int kl = 0; kl < ket.npp; ++kl) {
+        for (int kl = kl0; kl < kl1; ++kl) {
             const T* rk = reck + kl * SK;
             const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3), rq = __ldg(rk + 4);
             const T* ck = rk + 5;

@@ -107,14 +107,28 @@ __host__ __device__ inline int herm_index(int t, int u, int v)
 }
 
 // One unit of work: a shell quartet (bra pair, ket pair), restricted to the
-// bra primitive pairs [ij & 0xffff, ij >> 16).  Heavily contracted quartets
-// are split into several such chunks, each digested on its own (J and K are
-// linear in the integrals), so that no thread or warp carries a
-// disproportionate share of a launch.
-struct Task {
+// bra primitive pairs [i0, i1) and the ket primitive pairs [k0, k1).  A
+// quartet's primitive quartets can be split into any such tiles, each
+// digested on its own (J and K are linear in the integrals): heavily
+// contracted quartets are split so that no thread or warp carries a
+// disproportionate share of a launch, and launch groups with few quartets
+// are split further so that they still fill the GPU.  16 bytes, one vector
+// load.
+struct __align__(16) Task {
     int bra, ket;
-    int ij;
+    unsigned short i0, i1, k0, k1;
 };
+__host__ __device__ inline Task make_task(int bra, int ket, int i0, int i1, int k0, int k1)
+{
+    Task t;
+    t.bra = bra;
+    t.ket = ket;
+    t.i0 = (unsigned short)i0;
+    t.i1 = (unsigned short)i1;
+    t.k0 = (unsigned short)k0;
+    t.k1 = (unsigned short)k1;
+    return t;
+}
 
 // Arguments of the unique-ERI kernel (hfx_kernels.cu).
 struct LaunchArgs {

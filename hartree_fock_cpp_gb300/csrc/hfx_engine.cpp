@@ -507,7 +507,7 @@ void Job::compute_schwarz()
         int sl = warp_slice_elems(h.l0, h.l1, h.l0, h.l1, h.npp, kDefaultLaneMinNpp);
         int tier = 0;
         while ((512 << tier) < sl) ++tier;
-        tiers[tier].push_back({p, p, h.npp << 16});
+        tiers[tier].push_back(make_task(p, p, 0, h.npp, 0, h.npp));   // whole quartet: the pass writes, not adds
         tier_slice[tier] = std::max(tier_slice[tier], sl);
     }
     std::vector<DevBuf<Task>> dts(tiers.size());
@@ -599,7 +599,7 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     for_each_surviving_quartet(thr, [&](int X, int Y) {
         int bra = X, ket = Y;
         if (key(Y) > key(X)) std::swap(bra, ket);
-        tasks.push_back({bra, ket, hpairs_[bra].npp << 16});
+        tasks.push_back(make_task(bra, ket, 0, hpairs_[bra].npp, 0, hpairs_[ket].npp));
     });
     std::vector<double> c(tasks.size());
     double fsum = 0.0, psum = 0.0;
@@ -633,6 +633,8 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     auto pcof = [&](int p) { return pair_class(hpairs_[p].l0, hpairs_[p].l1); };
     // buckets: small classes per (pcb, pck, fp32); warp classes per (fp32)
     struct Bucket {
+        std::vector<std::pair<int, int>> q;   // surviving quartets (bra, ket)
+        double prims = 0.0;                   // their primitive quartets
         std::vector<Task> t;
         std::vector<double> cost;
     };
@@ -642,24 +644,56 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             int bra = X, ket = Y;
             if (pcof(Y) > pcof(X)) std::swap(bra, ket);
             const bool f32 = mixed && bound < tau;
-            const HostPair& b = hpairs_[bra];
-            const HostPair& k = hpairs_[ket];
-            const double fpp = flops_per_prim(b.l0, b.l1, k.l0, k.l1);
             const int pcb = pcof(bra), pck = pcof(ket);
             const bool sm = is_small_class(pcb, pck, f32);
             Bucket& bk = sm ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
-            // split the bra primitive pairs so that a chunk holds at most
-            // shape_.small_chunk primitive quartets (per thread) or
-            // shape_.warp_chunk (per warp)
-            const long long cap = sm ? shape_.small_chunk : shape_.warp_chunk;
-            const long long pq = (long long)b.npp * k.npp;
-            const int nch = (int)std::min<long long>(b.npp, std::max<long long>(1, (pq + cap - 1) / cap));
-            for (int c = 0; c < nch; ++c) {
-                const int i0 = (int)((long long)b.npp * c / nch), i1 = (int)((long long)b.npp * (c + 1) / nch);
-                bk.t.push_back({bra, ket, i0 | (i1 << 16)});
-                bk.cost.push_back((double)(i1 - i0) * k.npp * fpp);
-            }
+            bk.q.push_back({bra, ket});
+            bk.prims += (double)hpairs_[bra].npp * hpairs_[ket].npp;
     });
+    // Tiles of primitive quartets.  A thread task holds at most
+    // shape_.small_chunk primitive quartets and a warp task at most
+    // shape_.warp_chunk; a launch group with too few primitive quartets to
+    // give every SM several CTAs' worth of tasks at that size is cut finer
+    // (down to kMinThreadTile / kMinWarpTile), because a quartet list of a
+    // few thousand long tasks leaves most SMs idle.  Thread tasks split the
+    // bra primitive pairs first, then the ket ones; warp tasks split the bra
+    // primitive pairs only, so that each warp task keeps its whole ket
+    // contraction (the bra transform is applied once per bra primitive pair
+    // over the ket sum).
+    constexpr double kThreadFill = 4.0 * 128;   // threads per SM the thread-kernel groups should offer
+    constexpr double kWarpFill = 16.0;          // warps per SM for the warp-kernel groups
+    constexpr long long kMinThreadTile = 8, kMinWarpTile = 64;
+    auto tile = [&](Bucket& bk, bool sm) {
+        const double fill = (sm ? kThreadFill : kWarpFill) * nsm_;
+        const long long cap = sm ? shape_.small_chunk : shape_.warp_chunk;
+        const long long lo = sm ? kMinThreadTile : kMinWarpTile;
+        const long long c = std::max<long long>(std::min<long long>(lo, cap),
+                                                std::min<long long>(cap, (long long)std::ceil(bk.prims / fill)));
+        bk.t.reserve(bk.q.size());
+        bk.cost.reserve(bk.q.size());
+        for (const auto& bq : bk.q) {
+            const HostPair& b = hpairs_[bq.first];
+            const HostPair& k = hpairs_[bq.second];
+            const double fpp = flops_per_prim(b.l0, b.l1, k.l0, k.l1);
+            const long long pq = (long long)b.npp * k.npp;
+            const long long n = std::max<long long>(1, (pq + c - 1) / c);
+            const int nb = (int)std::min<long long>(b.npp, n);
+            const int nk = sm ? (int)std::min<long long>(k.npp, (n + nb - 1) / nb) : 1;
+            for (int x = 0; x < nb; ++x) {
+                const int i0 = (int)((long long)b.npp * x / nb), i1 = (int)((long long)b.npp * (x + 1) / nb);
+                for (int y = 0; y < nk; ++y) {
+                    const int k0 = (int)((long long)k.npp * y / nk), k1 = (int)((long long)k.npp * (y + 1) / nk);
+                    bk.t.push_back(make_task(bq.first, bq.second, i0, i1, k0, k1));
+                    bk.cost.push_back((double)(i1 - i0) * (k1 - k0) * fpp);
+                }
+            }
+        }
+        std::vector<std::pair<int, int>>().swap(bk.q);
+    };
+    for (auto& bk : small)
+        if (!bk.q.empty()) tile(bk, true);
+    for (auto& bk : warp)
+        if (!bk.q.empty()) tile(bk, false);
     std::vector<Task> all;
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();
@@ -680,7 +714,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 for (size_t i : sorted(bk)) {
                     all.push_back(bk.t[i]);
                     g.flops += bk.cost[i];
-                    g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * hpairs_[bk.t[i].ket].npp;
+                    g.prims += (double)(bk.t[i].i1 - bk.t[i].i0) * (bk.t[i].k1 - bk.t[i].k0);
                 }
                 groups.push_back(g);
             }
@@ -696,7 +730,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             const HostPair& k = hpairs_[bk.t[i].ket];
             // tier by slice size (powers of two), so that tasks with small
             // slices are not held to the occupancy of the largest one
-            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, shape_.lane_min_npp);
+            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, bk.t[i].k1 - bk.t[i].k0, shape_.lane_min_npp);
             int tier = 0;
             while ((512 << tier) < sl) ++tier;
             tiers[tier].push_back(i);
@@ -711,10 +745,11 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             for (size_t i : kv.second) {
                 const HostPair& b = hpairs_[bk.t[i].bra];
                 const HostPair& k = hpairs_[bk.t[i].ket];
-                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, k.npp, shape_.lane_min_npp));
+                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, bk.t[i].k1 - bk.t[i].k0,
+                                                         shape_.lane_min_npp));
                 all.push_back(bk.t[i]);
                 g.flops += bk.cost[i];
-                g.prims += (double)((bk.t[i].ij >> 16) - (bk.t[i].ij & 0xffff)) * k.npp;
+                g.prims += (double)(bk.t[i].i1 - bk.t[i].i0) * (bk.t[i].k1 - bk.t[i].k0);
             }
             g.slice = (slice + 1) & ~1;
             g.lane_min_npp = shape_.lane_min_npp;
@@ -731,7 +766,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         if (g.fp32) {
             gs.flops32 += g.flops;
             for (size_t i = g.off; i < g.off + g.n; ++i)
-                if ((all[i].ij & 0xffff) == 0) gs.quartets32 += 1.0;
+                if (all[i].i0 == 0 && all[i].k0 == 0) gs.quartets32 += 1.0;
         } else {
             gs.flops64 += g.flops;
         }
@@ -740,7 +775,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     gs.ntasks = (int)all.size();
     gs.nquartets = 0;
     for (const auto& t : all)
-        if ((t.ij & 0xffff) == 0) ++gs.nquartets;
+        if (t.i0 == 0 && t.k0 == 0) ++gs.nquartets;
     gs.tasks.upload(all, stream_);
 }
 

@@ -254,6 +254,8 @@ public:
     // pick the launch shape by timing builds at density P (host, K x K); returns the best build ms
     double autotune_launch_shape(const double* P, int builds, hfx_launch_shape* out);
     int num_launch_groups() const { return (int)plan(true).groups.size(); }
+    // launch groups of a plan (FP64 or, for a mixed job, mixed)
+    const std::vector<LaunchGroup>& plan_groups(bool mixed_plan) const { return plan(mixed_plan).groups; }
     void fock_uhf_device(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb);
     void fock_rhf(const double* P, double* G);
     void fock_uhf(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb);

@@ -250,19 +250,20 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
         T* acc = sl;
         T* W = acc + nout;
         T* Ra = W + nw;
-        const bool lane_mode = a.lane_min_npp > 0 && L <= 6 && ket.npp >= a.lane_min_npp;
+        const int kl_begin = task.k0, kl_end = task.k1, nkl = kl_end - kl_begin;
+        const bool lane_mode = a.lane_min_npp > 0 && L <= 6 && nkl >= a.lane_min_npp;
         T* Sd = Ra + (lane_mode ? HL * 32 : (2 + kWarpKetRound) * HL);   // seeds: (L+1) x 32 (lane mode) or L+1
         for (int e = lane; e < nout; e += 32) acc[e] = (T)0;
 
-        const int ij_end = task.ij >> 16;
-        for (int ij = task.ij & 0xffff; ij < ij_end; ++ij) {
+        const int ij_end = task.i1;
+        for (int ij = task.i0; ij < ij_end; ++ij) {
             const T* rb = rec + bra.rec_off + (long long)ij * cb.stride;
             const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
             for (int e = lane; e < nw; e += 32) W[e] = (T)0;
             __syncwarp();
             if (lane_mode) {
-                for (int kl0 = 0; kl0 < ket.npp; kl0 += 32) {
-                    const int nb = min(32, ket.npp - kl0);
+                for (int kl0 = kl_begin; kl0 < kl_end; kl0 += 32) {
+                    const int nb = min(32, kl_end - kl0);
                     if (lane < nb) {
                         const T* rk = rec + ket.rec_off + (long long)(kl0 + lane) * ck.stride;
                         const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),
@@ -303,8 +304,8 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 // slot of Rb), then one ket transform over the round that reads
                 // each coefficient's Hermite offset and sign once
                 T* Rb = Ra + 2 * HL;
-                for (int kl0 = 0; kl0 < ket.npp; kl0 += kWarpKetRound) {
-                    const int nb = min(kWarpKetRound, ket.npp - kl0);
+                for (int kl0 = kl_begin; kl0 < kl_end; kl0 += kWarpKetRound) {
+                    const int nb = min(kWarpKetRound, kl_end - kl0);
                     for (int b = 0; b < nb; ++b) {
                         const T* rk = rec + ket.rec_off + (long long)(kl0 + b) * ck.stride;
                         const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3),

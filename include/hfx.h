@@ -282,6 +282,14 @@ hfx_status hfx_debug_pair_data(const hfx_molecule *mol, int *npairs, int *nprimp
  * and offs[3*p ..] = moff, qoff, npp.  Pass rec = offs = NULL to get npairs. */
 hfx_status hfx_debug_packed_pairs(const hfx_molecule *mols, int n, int *npairs, int *rec, long long *offs);
 
+/* Test hook (no device work): the launch groups of a job's Fock-build plan
+ * (mixed != 0: the mixed-precision plan of a mixed job), 10 doubles per
+ * group: kind (0 thread-per-quartet class kernel, 1 warp kernel), bra and
+ * ket pair class (class kernels), fp32, tasks, algorithmic flops, primitive
+ * quartets, grid, shared-memory slice and warps per CTA (warp kernel).
+ * Pass rows = NULL to get ngroups.  No counterpart in the reference. */
+hfx_status hfx_debug_plan(const hfx_job *job, int mixed, int *ngroups, double *rows);
+
 /* One-electron matrices S, T, V of a molecule (integrals.hpp:10-536), host. */
 hfx_status hfx_one_electron(const hfx_molecule *mol, double *S, double *T, double *V, int *K);
 /* The same matrices computed on CUDA device `device` (one CTA per shell pair;
@@ -357,16 +365,21 @@ hfx_status hfx_server_destroy(hfx_server *server);
  * iterate in lockstep: each SCF cycle is ONE Fock build over every molecule
  * still iterating (one launch per quartet class over all molecules'
  * quartets, replayed as a CUDA graph), each molecule's O(K^3) SCF steps run
- * on its own stream.  Every molecule starts from the zero density (the
- * reference's sequential scan warm-starts from the previous geometry).
+ * on its own stream.  With warm_chain = 0 or 1 every molecule starts from
+ * the zero density.  With warm_chain = c > 1 the molecules form chains of c
+ * consecutive indices (0..c-1, c..2c-1, ...): inside a chain molecule i
+ * starts from molecule i-1's final density, as the reference's sequential
+ * scan does from the previous geometry (run.hpp:353-368), so a chain's
+ * molecules run one after another while the chains iterate together.
  * One method per batch; UHF takes per-molecule n_alpha[i], n_beta[i].
  * results[i] gets molecule i's result.  HFX_ERR_NOT_CONVERGED if some
  * molecule did not converge (every result still filled); any other failure
  * returns the first failing molecule's status. */
 typedef struct {
     int method;              /* 0 RHF, 1 UHF */
-    int max_parallel;        /* molecules iterating at once (0: all, at most 256) */
-    int reserved[6];
+    int max_parallel;        /* molecules (chains, with warm_chain > 1) iterating at once (0: all, at most 256) */
+    int warm_chain;          /* > 1: warm-started chains of this many consecutive molecules (above) */
+    int reserved[5];
 } hfx_batch_options;
 
 typedef struct {

@@ -54,3 +54,42 @@ def test_batch_mixed_precision_within_1uha_of_fp64():
         assert a["converged"] and b["converged"]
         assert abs(a["E_tot"] - b["E_tot"]) < E_TOL
     assert sum(b["mixed_builds"] for b in rmx) > 0
+
+
+def test_batch_warm_chains_match_sequential_warm_started_scan():
+    """warm_chain = 3: chains of three consecutive scan points, each point
+    starting from the previous point's final density while the chains iterate
+    together; every point matches the sequential scan that starts each point
+    from the previous one (run_bl_scan, run.hpp:353-368) in energy (1 uHa)
+    and iteration count (+-1)."""
+    pts = W.water_scan(6)
+    mols = [(cfg, "cc-pVDZ") for cfg in pts]
+    res, st = H.batch_scf(mols, warm_chain=3)
+    assert st["molecules"] == 6
+    for chain in (range(0, 3), range(3, 6)):
+        P = None
+        for i in chain:
+            a = H.rhf_diis(pts[i], "cc-pVDZ", set_initial_density=P is not None, P0=P)
+            P = a["density"]
+            r = res[i]
+            assert r["converged"] and a["converged"]
+            assert abs(r["E_tot"] - a["E_tot"]) < E_TOL
+            assert abs(r["iterations"] - a["iterations"]) <= 1, (i, r["iterations"], a["iterations"])
+    # warm-started points need fewer iterations than the chain heads
+    assert res[1]["iterations"] < res[0]["iterations"]
+
+
+def test_batch_warm_chain_matches_reference_loop_fixture():
+    """Two consecutive water/cc-pVTZ scan points in one chain: the second
+    point's iteration count is the reference loop's warm-started count
+    (tests/golden/scf_golden.json, from the reference's own tensor)."""
+    import json
+    import os
+    g = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scf_golden.json")))
+    head, warm = g["water_ccpvtz_20"], g["water_ccpvtz_21_warm"]
+    cfg = lambda c: [(s, tuple(x)) for s, x in c["config"]]
+    res, _ = H.batch_scf([(cfg(head), "cc-pVTZ"), (cfg(warm), "cc-pVTZ")], warm_chain=2)
+    assert abs(res[0]["E_tot"] - head["E_tot"]) < E_TOL
+    assert abs(res[0]["iterations"] - head["iterations"]) <= 1
+    assert abs(res[1]["E_tot"] - warm["E_tot"]) < E_TOL
+    assert abs(res[1]["iterations"] - warm["iterations"]) <= 1, (res[1]["iterations"], warm["iterations"])
