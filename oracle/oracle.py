@@ -622,3 +622,44 @@ class RefLib:
         S, T, V = np.zeros((K, K)), np.zeros((K, K)), np.zeros((K, K))
         self.L.ref_one_electron(_ptr(S), _ptr(T), _ptr(V))
         return S, T, V
+
+
+class RefGridLib:
+    """The reference's own cube.hpp grid evaluation via
+    oracle/_ref/libhfref_grid.so (only where a checkout of the reference was
+    available at build time)."""
+
+    def __init__(self):
+        path = os.path.join(HERE, "_ref", "libhfref_grid.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        L = ctypes.CDLL(path)
+        L.refg_build_basis.restype = ctypes.c_int
+        L.refg_build_basis.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p,
+                                       ctypes.c_char_p]
+        L.refg_points.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.refg_box_points.argtypes = [ctypes.c_double] * 4 + [ctypes.c_int, ctypes.c_void_p]
+        self.L = L
+        self.K = 0
+
+    def build(self, config, basis_set, basis_path=BASIS_PATH):
+        syms = (ctypes.c_char_p * len(config))(*[s.encode() for s, _ in config])
+        xyz = np.ascontiguousarray(np.array([R for _, R in config], dtype=np.float64).reshape(-1))
+        K = self.L.refg_build_basis(len(config), ctypes.cast(syms, ctypes.c_void_p), _ptr(xyz),
+                                    basis_set.encode(), basis_path.encode())
+        if K < 0:
+            raise RuntimeError("reference basis_construction failed")
+        self.K = K
+        return K
+
+    def points(self, M, column, xyz):
+        M = np.ascontiguousarray(M, dtype=np.float64)
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(len(xyz))
+        self.L.refg_points(_ptr(M), int(column), _ptr(xyz), len(xyz), _ptr(out))
+        return out
+
+    def box_points(self, center, L, res):
+        out = np.zeros((res ** 3, 3))
+        self.L.refg_box_points(float(center[0]), float(center[1]), float(center[2]), float(L), int(res), _ptr(out))
+        return out

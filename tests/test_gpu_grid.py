@@ -53,3 +53,28 @@ def test_points_and_density_of_a_converged_scf_integrates_to_n_electrons(tmp_pat
     lines = open(f).read().splitlines()
     assert lines[2].split()[0] == "3" and lines[3].split()[0] == "4"
     assert len(lines[6 + 3].split()) == 6
+
+
+def test_grid_kernels_match_reference_golden():
+    """Box grids and explicit points on the GPU against the reference's own
+    cube.hpp evaluation (tests/golden/grid_golden.json): 1e-12 relative to the
+    field's largest value."""
+    import json
+    g = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "grid_golden.json")))
+    for c in g:
+        cfg = [(s, tuple(x)) for s, x in c["config"]]
+        b = H.basis_construction(cfg, c["basis"])
+        K = b.K
+        i, j = np.meshgrid(np.arange(K), np.arange(K), indexing="ij")
+        P = np.cos(0.37 * i + 0.53 * j) + np.cos(0.37 * j + 0.53 * i)
+        C = np.sin(0.11 * i * j + 0.7 * i)
+        rho = cube.density3d(b, P, tuple(c["center"]), c["L"], c["res"])["field"].ravel()
+        psi = cube.orbital3d(b, C, c["column"], tuple(c["center"]), c["L"], c["res"])["field"].ravel()
+        for got, ref in ((rho, c["rho_box"]), (psi, c["psi_box"])):
+            ref = np.array(ref)
+            assert np.abs(got - ref).max() < 1e-12 * max(1.0, np.abs(ref).max())
+        pts = np.array(c["points"])
+        for got, ref in ((cube.points_eval(b, P, pts), c["rho_points"]),
+                         (cube.points_eval(b, C, pts, index=c["column"]), c["psi_points"])):
+            ref = np.array(ref)
+            assert np.abs(got - ref).max() < 1e-12 * max(1.0, np.abs(ref).max())

@@ -96,3 +96,31 @@ def test_reference_library_if_present():
     for _ in range(20):
         i, j, k, l = (int(x) for x in rng.integers(0, orc.K, 4))
         assert orc.eri(i, j, k, l) == r.eri(i, j, k, l)
+
+
+def _grid_golden():
+    import json
+    return json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "grid_golden.json")))
+
+
+def _grid_matrices(K):
+    # the closed-form matrices of tests/golden/make_grid_golden.py
+    i, j = np.meshgrid(np.arange(K), np.arange(K), indexing="ij")
+    return np.cos(0.37 * i + 0.53 * j) + np.cos(0.37 * j + 0.53 * i), np.sin(0.11 * i * j + 0.7 * i)
+
+
+def test_grid_restatement_matches_reference_golden():
+    """The oracle's restatement of function_eval / electron_density /
+    orbital_wf / box_points (cube.hpp:9-168) against the reference's own code
+    (tests/golden/grid_golden.json, cube.hpp compiled unchanged)."""
+    for c in _grid_golden():
+        fb = O.FlatBasis([(s, tuple(x)) for s, x in c["config"]], c["basis"])
+        assert fb.K == c["K"]
+        P, C = _grid_matrices(fb.K)
+        box = O.box_points(c["center"], c["L"], c["res"])
+        assert np.array_equal(box, np.array(c["box"]))
+        for pts, rho, psi in ((box, c["rho_box"], c["psi_box"]), (np.array(c["points"]), c["rho_points"],
+                                                                  c["psi_points"])):
+            rho, psi = np.array(rho), np.array(psi)
+            assert np.abs(O.electron_density(fb, P, pts) - rho).max() < 1e-13 * np.abs(rho).max()
+            assert np.abs(O.orbital_wf(fb, C, c["column"], pts) - psi).max() < 1e-13 * max(1.0, np.abs(psi).max())
