@@ -536,21 +536,23 @@ def serve_section(H, W, n_jobs, device, rate_factors=(1.0, 2.0, 4.0), tau=0.03, 
                 infos = [srv.poll(i) for i in ids]
                 st = srv.stats()
             lat = [i["t_end"] - i["t_submit"] for i in infos]
+            extra = {"max_session_members": st["max_session_members"]} if pack_max > 1 else {}
             ok = sum(1 for i in infos if i["converged"])
             dE = [abs(i["E_tot"] - e) for i, e in zip(infos, seq_E) if e is not None and i["converged"]]
             return {"solves_per_s": ok / T_srv, "jobs_per_s": n_jobs / T_srv,
                     "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                     "converged": ok, "max_concurrent": st["max_concurrent"], "fp32_threshold": tau,
-                    "max_abs_dE_vs_fp64": float(max(dE)) if dE else None}
+                    "max_abs_dE_vs_fp64": float(max(dE)) if dE else None, **extra}
         entry = {
             "arrival_rate_x": rf, "arrival_span_s": float(arrivals[-1]),
             "one_at_a_time_fp64": {"solves_per_s": seq_ok / free_at,
                                    "p50_s": float(np.percentile(seq_resp, 50)),
                                    "p99_s": float(np.percentile(seq_resp, 99))},
             "served_mixed": serve(0)}
-        if rf == max(rate_factors):
-            # packed mode: up to 8 requests of one method per worker, lockstep on one packed job
-            entry["served_mixed_packed8"] = serve(8)
+        if rf >= 2.0:
+            # packed mode: running requests share Fock sessions (up to 8 members per
+            # method, options and size class; one launch per class per cycle)
+            entry["served_mixed_packed"] = serve(8)
         out["rates"].append(entry)
     return out
 

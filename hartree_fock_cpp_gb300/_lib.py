@@ -91,7 +91,8 @@ class JobInfo(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("queued", ctypes.c_int), ("running", ctypes.c_int), ("done", ctypes.c_int), ("failed", ctypes.c_int),
                 ("max_concurrent", ctypes.c_int), ("budget_bytes", ctypes.c_double),
-                ("in_use_bytes", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
+                ("in_use_bytes", ctypes.c_double), ("max_session_members", ctypes.c_int),
+                ("sessions_created", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class BatchOptions(ctypes.Structure):

@@ -57,6 +57,54 @@ __host__ __device__ constexpr int hidx(int t, int u, int v)
     return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 + t * (t + u + v + 1) - t * (t - 1) / 2 + u;
 }
 
+// (t, u, v) of packed Hermite index h (inverse of hidx): s-major, then t, then u.
+__host__ __device__ constexpr int herm_s(int h)
+{
+    int s = 0;
+    while ((s + 1) * (s + 2) * (s + 3) / 6 <= h) ++s;
+    return s;
+}
+__host__ __device__ constexpr int herm_t(int h)
+{
+    int s = herm_s(h), o = h - s * (s + 1) * (s + 2) / 6, t = 0;
+    while (o >= s - t + 1) {
+        o -= s - t + 1;
+        ++t;
+    }
+    return t;
+}
+__host__ __device__ constexpr int herm_u(int h)
+{
+    int s = herm_s(h), t = herm_t(h);
+    return h - s * (s + 1) * (s + 2) / 6 - (t * (s + 1) - t * (t - 1) / 2);
+}
+__host__ __device__ constexpr int herm_v(int h) { return herm_s(h) - herm_t(h) - herm_u(h); }
+__host__ __device__ constexpr bool herm_inverse_ok()
+{
+    for (int h = 0; h < 455; ++h)
+        if (hidx(herm_t(h), herm_u(h), herm_v(h)) != h || herm_u(h) < 0 || herm_v(h) < 0) return false;
+    return true;
+}
+static_assert(herm_inverse_ok(), "packed Hermite index inverse");
+
+// Compile-time loops: cfor<B, E>(f) calls f(CInt<B>{}) ... f(CInt<E-1>{}), so
+// that every index inside f is a constant expression.  The class kernels
+// index their register arrays (R, the ket sums, the accumulators) only
+// through such constants; a loop the compiler declined to unroll would turn
+// them into local-memory arrays.
+template <int V>
+struct CInt {
+    static constexpr int value = V;
+};
+template <int B, int E, typename F>
+__device__ __forceinline__ void cfor(F&& f)
+{
+    if constexpr (B < E) {
+        f(CInt<B>{});
+        cfor<B + 1, E>(f);
+    }
+}
+
 // number of non-zero coefficients of component pair ab of a (la, lb) pair
 __host__ __device__ constexpr int n_coef_ab(int la, int lb, int ab)
 {
@@ -130,32 +178,33 @@ template <typename T, int L>
 __device__ __forceinline__ void hermite_R(T X, T Y, T Z, const T (&s)[L + 1], T (&R)[c_nh(L)])
 {
     R[0] = s[L];
-#pragma unroll
-    for (int n = L - 1; n >= 0; --n) {
-#pragma unroll
-        for (int sl = L - n; sl >= 1; --sl) {
-#pragma unroll
-            for (int t = 0; t <= sl; ++t) {
-#pragma unroll
-                for (int u = 0; u <= sl - t; ++u) {
-                    const int v = sl - t - u;
+    cfor<0, L>([&](auto ic) {
+        constexpr int n = L - 1 - decltype(ic)::value;
+        // levels L-n down to 1, each from the two levels below it (still
+        // holding the values of order n+1)
+        cfor<0, L - n>([&](auto jc) {
+            constexpr int sl = L - n - decltype(jc)::value;
+            cfor<0, sl + 1>([&](auto tc) {
+                constexpr int t = decltype(tc)::value;
+                cfor<0, sl - t + 1>([&](auto uc) {
+                    constexpr int u = decltype(uc)::value, v = sl - t - u;
                     T val;
-                    if (t > 0) {
+                    if constexpr (t > 0) {
                         val = X * R[hidx(t - 1, u, v)];
-                        if (t > 1) val = fma((T)(t - 1), R[hidx(t - 2, u, v)], val);
-                    } else if (u > 0) {
+                        if constexpr (t > 1) val = fma((T)(t - 1), R[hidx(t - 2, u, v)], val);
+                    } else if constexpr (u > 0) {
                         val = Y * R[hidx(t, u - 1, v)];
-                        if (u > 1) val = fma((T)(u - 1), R[hidx(t, u - 2, v)], val);
+                        if constexpr (u > 1) val = fma((T)(u - 1), R[hidx(t, u - 2, v)], val);
                     } else {
                         val = Z * R[hidx(t, u, v - 1)];
-                        if (v > 1) val = fma((T)(v - 1), R[hidx(t, u, v - 2)], val);
+                        if constexpr (v > 1) val = fma((T)(v - 1), R[hidx(t, u, v - 2)], val);
                     }
                     R[hidx(t, u, v)] = val;
-                }
-            }
-        }
+                });
+            });
+        });
         R[0] = s[n];
-    }
+    });
 }
 
 __device__ __forceinline__ long long spidx(int a, int b)
@@ -163,6 +212,11 @@ __device__ __forceinline__ long long spidx(int a, int b)
     int hi = a > b ? a : b, lo = a > b ? b : a;
     return (long long)hi * (hi + 1) / 2 + lo;
 }
+
+// Register bytes per thread for the ket sum Wt of the amortised bra
+// transform (below this the class sums over the ket primitive pairs before
+// the bra transform).
+constexpr int kAmortizeBytes = 256;
 
 template <typename T, int LA, int LB, int LC, int LD, int NK>
 __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
@@ -172,6 +226,8 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
     constexpr int NAB = c_nc(LA) * NB, NCD = c_nc(LC) * ND;
     constexpr int H1 = c_nh(L1), HL = c_nh(L);
     constexpr int SB = rec_stride(LA, LB), SK = rec_stride(LC, LD);
+    // amortised bra transform when the ket sum fits in registers beside acc
+    constexpr bool AMB = NCD * H1 * (int)sizeof(T) <= kAmortizeBytes;
 
     const int task = blockIdx.x * blockDim.x + threadIdx.x;
     if (task >= a.ntasks) return;
@@ -194,6 +250,19 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
         const T* rb = recb + ij * SB;
         const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
         const T* cb = rb + 5;
+        // kAmortizeBra: the ket-transformed integrals of every ket component
+        // pair are summed over the task's ket primitive pairs first
+        // (Wt[cd][tuv], in registers), and the bra transform is applied once
+        // per bra primitive pair -- each bra coefficient is loaded once and
+        // used for every cd.  Otherwise (classes whose Wt would not fit the
+        // register file) the bra transform runs per primitive quartet.
+        T Wt[AMB ? NCD : 1][AMB ? H1 : 1];
+        if constexpr (AMB) {
+#pragma unroll
+            for (int cd = 0; cd < NCD; ++cd)
+#pragma unroll
+                for (int h = 0; h < H1; ++h) Wt[cd][h] = (T)0;
+        }
         for (int kl = kl0; kl < kl1; ++kl) {
             const T* rk = reck + kl * SK;
             const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3), rq = __ldg(rk + 4);
@@ -218,49 +287,75 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             }
             T R[HL];
             hermite_R<T, L>(X, Y, Z, sd, R);
+            cfor<0, NCD>([&](auto cdc) {
+                constexpr int cd = decltype(cdc)::value;
+                constexpr int c = cd / ND, d = cd % ND;
+                constexpr int nx = comp_x(LC, c) + comp_x(LD, d), ny = comp_y(LC, c) + comp_y(LD, d),
+                              nz = comp_z(LC, c) + comp_z(LD, d);
+                constexpr int k0 = coef_off(LC, LD, cd);
+                T W[AMB ? 1 : H1];
+                if constexpr (!AMB) {
 #pragma unroll
-            for (int cd = 0; cd < NCD; ++cd) {
-                const int c = cd / ND, d = cd % ND;
-                const int nx = comp_x(LC, c) + comp_x(LD, d), ny = comp_y(LC, c) + comp_y(LD, d),
-                          nz = comp_z(LC, c) + comp_z(LD, d);
-                T W[H1];
-#pragma unroll
-                for (int h = 0; h < H1; ++h) W[h] = (T)0;
-                int k = coef_off(LC, LD, cd);
-#pragma unroll
-                for (int tn = 0; tn <= nx; ++tn)
-#pragma unroll
-                    for (int nu = 0; nu <= ny; ++nu)
-#pragma unroll
-                        for (int ph = 0; ph <= nz; ++ph, ++k) {
-                            T e = __ldg(ck + k);
-                            if ((tn + nu + ph) & 1) e = -e;
-#pragma unroll
-                            for (int s1 = 0; s1 <= L1; ++s1)
-#pragma unroll
-                                for (int t = 0; t <= s1; ++t)
-#pragma unroll
-                                    for (int u = 0; u <= s1 - t; ++u) {
-                                        const int v = s1 - t - u;
-                                        W[hidx(t, u, v)] = fma(e, R[hidx(t + tn, u + nu, v + ph)], W[hidx(t, u, v)]);
-                                    }
-                        }
-#pragma unroll
-                for (int ab = 0; ab < NAB; ++ab) {
-                    const int aa = ab / NB, bb = ab % NB;
-                    const int mx = comp_x(LA, aa) + comp_x(LB, bb), my = comp_y(LA, aa) + comp_y(LB, bb),
-                              mz = comp_z(LA, aa) + comp_z(LB, bb);
-                    int kb = coef_off(LA, LB, ab);
-                    T s = acc[ab][cd];
-#pragma unroll
-                    for (int t = 0; t <= mx; ++t)
-#pragma unroll
-                        for (int u = 0; u <= my; ++u)
-#pragma unroll
-                            for (int v = 0; v <= mz; ++v, ++kb) s = fma(__ldg(cb + kb), W[hidx(t, u, v)], s);
-                    acc[ab][cd] = s;
+                    for (int h = 0; h < H1; ++h) W[h] = (T)0;
                 }
-            }
+                // W_cd[tuv] (+)= sum_{tnp in nz(cd)} (-1)^{|tnp|} c_{cd,tnp} R[tuv + tnp]
+                cfor<0, nx + 1>([&](auto tnc) {
+                    constexpr int tn = decltype(tnc)::value;
+                    cfor<0, ny + 1>([&](auto nuc) {
+                        constexpr int nu = decltype(nuc)::value;
+                        cfor<0, nz + 1>([&](auto phc) {
+                            constexpr int ph = decltype(phc)::value;
+                            constexpr int k = k0 + (tn * (ny + 1) + nu) * (nz + 1) + ph;
+                            T e = __ldg(ck + k);
+                            if constexpr ((tn + nu + ph) & 1) e = -e;
+                            cfor<0, H1>([&](auto hc) {
+                                constexpr int h = decltype(hc)::value;
+                                constexpr int t = herm_t(h), u = herm_u(h), v = herm_v(h);
+                                constexpr int r = hidx(t + tn, u + nu, v + ph);
+                                if constexpr (AMB)
+                                    Wt[cd][h] = fma(e, R[r], Wt[cd][h]);
+                                else
+                                    W[h] = fma(e, R[r], W[h]);
+                            });
+                        });
+                    });
+                });
+                if constexpr (!AMB) {
+                    cfor<0, NAB>([&](auto abc) {
+                        constexpr int ab = decltype(abc)::value;
+                        constexpr int aa = ab / NB, bb = ab % NB;
+                        constexpr int mx = comp_x(LA, aa) + comp_x(LB, bb), my = comp_y(LA, aa) + comp_y(LB, bb),
+                                      mz = comp_z(LA, aa) + comp_z(LB, bb);
+                        constexpr int kb0 = coef_off(LA, LB, ab);
+                        T sacc = acc[ab][cd];
+                        cfor<0, (mx + 1) * (my + 1) * (mz + 1)>([&](auto jc) {
+                            constexpr int j = decltype(jc)::value;
+                            constexpr int t = j / ((my + 1) * (mz + 1)), u = (j / (mz + 1)) % (my + 1), v = j % (mz + 1);
+                            sacc = fma(__ldg(cb + kb0 + j), W[hidx(t, u, v)], sacc);
+                        });
+                        acc[ab][cd] = sacc;
+                    });
+                }
+            });
+        }
+        if constexpr (AMB) {
+            // bra transform of the ket sum, once per bra primitive pair
+            cfor<0, NAB>([&](auto abc) {
+                constexpr int ab = decltype(abc)::value;
+                constexpr int aa = ab / NB, bb = ab % NB;
+                constexpr int mx = comp_x(LA, aa) + comp_x(LB, bb), my = comp_y(LA, aa) + comp_y(LB, bb),
+                              mz = comp_z(LA, aa) + comp_z(LB, bb);
+                constexpr int kb0 = coef_off(LA, LB, ab);
+                cfor<0, (mx + 1) * (my + 1) * (mz + 1)>([&](auto jc) {
+                    constexpr int j = decltype(jc)::value;
+                    constexpr int t = j / ((my + 1) * (mz + 1)), u = (j / (mz + 1)) % (my + 1), v = j % (mz + 1);
+                    const T cv = __ldg(cb + kb0 + j);
+                    cfor<0, NCD>([&](auto cdc) {
+                        constexpr int cd = decltype(cdc)::value;
+                        acc[ab][cd] = fma(cv, Wt[cd][hidx(t, u, v)], acc[ab][cd]);
+                    });
+                });
+            });
         }
     }
 

@@ -23,6 +23,7 @@ KernelSpec finish_uhf_spec(int Kmax, int nfrag);   // k_finish_uhf(Jacc, Ka, Kb,
 KernelSpec add_spec(long long n);    // k_add(A, B, C, n)
 KernelSpec to_float_spec(long long n);   // k_to_float(A, B, n)
 KernelSpec density_blocks_spec(int npairs);   // k_density_blocks(pairs, npairs, D1, D2, Dsh)
+KernelSpec rebase_tasks_spec(long long n);    // k_rebase_tasks(tasks, n, delta): bra, ket += delta
 cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<double>)
 cudaError_t small_spec_f32(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // k_small(SmallArgs<float>)
 cudaError_t warp_spec(bool fp32, int nk, int grid, int warps_per_cta, int slice, KernelSpec* s);
@@ -206,7 +207,11 @@ public:
     virtual double last_build_ms() const = 0;   // device time of the last build
 };
 
+class FockSession;
+
 class Job final : public FockSource {
+    friend class FockSession;   // reads the device pair tables and plans of its members
+
 public:
     Job(Basis b, const hfx_options& opt);
     // Packed job over several molecules: shell pairs and quartets never mix
@@ -238,6 +243,7 @@ public:
     void fock_uhf_ex(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, bool mixed, double dthr);
     bool mixed() const override { return opt_.precision == HFX_PREC_MIXED; }
     double fp32_threshold() const { return opt_.fp32_threshold; }
+    double screening_threshold() const { return opt_.screening_threshold; }
     // Pick the FP32 threshold: for each candidate (largest first) build G in
     // mixed precision at density P and keep the largest tau whose energy
     // change 1/2 sum P (G_tau - G_fp64) stays within target_dE; the job is

@@ -358,6 +358,17 @@ KernelSpec finish_uhf_spec(int Kmax, int nfrag)
 {
     return elementwise_spec((const void*)k_finish_uhf, (long long)Kmax * Kmax, nfrag);
 }
+// Shift the pair indices of a task list copied into a combined list (the
+// multi-job Fock session, hfx_session.cpp).
+__global__ void k_rebase_tasks(Task* t, long long n, int delta)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        t[i].bra += delta;
+        t[i].ket += delta;
+    }
+}
+
+KernelSpec rebase_tasks_spec(long long n) { return elementwise_spec((const void*)k_rebase_tasks, n, 1); }
 KernelSpec add_spec(long long n) { return elementwise_spec((const void*)k_add, n, 1); }
 KernelSpec to_float_spec(long long n) { return elementwise_spec((const void*)k_to_float, n, 1); }
 

@@ -12,11 +12,14 @@
 // step overlaps the others' GPU work.  Jobs finish, free their slot and
 // budget, and queued requests are admitted in their place.
 //
-// Packed mode (pack_max > 1): a worker that admits a request also admits up
-// to pack_max - 1 further queued requests of the same method and precision,
-// and runs them in lockstep on one packed job (run_packed, hfx_batch.cpp):
-// every SCF cycle is one Fock build for all of them.  Each job leaves the
-// pack, posts its result and frees its budget as soon as its own SCF ends.
+// Packed mode (pack_max > 1): every admitted request still builds its own
+// job on its worker, then joins a Fock session (hfx_session.cpp) shared with
+// the running requests of the same method, options and size class: from its
+// next SCF cycle on, its quartets are part of the session's launches -- one
+// launch per quartet class per cycle over all members.  A request that
+// arrives while others iterate is admitted as soon as a worker slot and
+// memory are free and enters the running builds; each member leaves when
+// its own SCF ends (at most pack_max members per session).
 //
 // Failures stay with the job that caused them: a bad basis file, an
 // unsupported element, a footprint above the whole budget, an allocation
@@ -38,6 +41,7 @@
 #include "hfx_dscf.hpp"
 #include "hfx_engine.hpp"
 #include "hfx_scf.hpp"
+#include "hfx_session.hpp"
 
 namespace hfx {
 
@@ -70,6 +74,48 @@ struct ServerJob {
     size_t footprint = 0;
     std::vector<double> Pa, Pb;
     std::atomic<bool> cancel{false};
+};
+
+// A server job's view of its Fock session, as the device SCF sees a builder.
+class SessionMember final : public FockSource {
+public:
+    explicit SessionMember(const Job& job) : K_(job.K()), mixed_(job.mixed())
+    {
+        cuda_check(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
+    ~SessionMember() override
+    {
+        if (st_) {
+            cudaStreamSynchronize(st_);
+            cudaStreamDestroy(st_);
+        }
+    }
+    void attach(FockSession* s, int slot)
+    {
+        s_ = s;
+        slot_ = slot;
+    }
+    int K() const override { return K_; }
+    cudaStream_t stream() const override { return st_; }
+    bool mixed() const override { return mixed_; }
+    void fock_rhf_device_ex(const double* dP, double* dG, bool mixed, double dthr) override
+    {
+        s_->build(slot_, st_, dP, nullptr, dG, nullptr, nullptr, mixed, dthr, &ms_);
+    }
+    void fock_uhf_device_ex(const double* dPa, const double* dPb, double* dJ, double* dKa, double* dKb, bool mixed,
+                            double dthr) override
+    {
+        s_->build(slot_, st_, dPa, dPb, dJ, dKa, dKb, mixed, dthr, &ms_);
+    }
+    double last_build_ms() const override { return ms_; }
+
+private:
+    FockSession* s_ = nullptr;
+    int slot_ = -1;
+    int K_;
+    bool mixed_;
+    cudaStream_t st_ = nullptr;
+    double ms_ = 0.0;
 };
 
 class Server {
@@ -110,6 +156,10 @@ public:
         j->scf = r.scf;
         j->precision = r.precision < 0 ? opt_.precision : r.precision;
         j->fp32_threshold = r.fp32_threshold > 0 ? r.fp32_threshold : opt_.fp32_threshold;
+        // the SCF follows the job's precision: a mixed-precision job runs the
+        // mixed-precision protocol (FP32 builds, then FP64 final cycles)
+        j->scf.precision = j->precision;
+        j->scf.fp32_threshold = j->fp32_threshold;
         j->timeout_s = r.timeout_s;
         j->inject_fault = r.inject_fault;
         j->t_submit = now_s();
@@ -180,6 +230,8 @@ public:
         s->budget_bytes = (double)budget_;
         s->in_use_bytes = (double)in_use_;
         s->max_concurrent = max_concurrent_;
+        s->max_session_members = max_session_members_;
+        s->sessions_created = sessions_created_;
         for (auto& kv : jobs_) {
             if (kv.second->state == HFX_JOB_DONE) ++s->done;
             if (kv.second->state == HFX_JOB_FAILED) ++s->failed;
@@ -249,27 +301,6 @@ private:
                 ++running_;
                 j->state = HFX_JOB_RUNNING;
                 j->t_admit = now_s();
-                if (opt_.pack_max > 1) {
-                    std::vector<std::shared_ptr<ServerJob>> pack{j};
-                    for (auto it = queue_.begin(); it != queue_.end() && (int)pack.size() < opt_.pack_max;) {
-                        auto& c = *it;
-                        if (!c->cancel && same_job_options(*c, *j)) {
-                            c->state = HFX_JOB_RUNNING;
-                            c->t_admit = now_s();
-                            ++running_;
-                            pack.push_back(c);
-                            it = queue_.erase(it);
-                        } else {
-                            ++it;
-                        }
-                    }
-                    max_concurrent_ = std::max(max_concurrent_, running_);
-                    if (pack.size() > 1) {
-                        lk.unlock();
-                        run_pack(pack);
-                        continue;
-                    }
-                }
                 max_concurrent_ = std::max(max_concurrent_, running_);
             }
             run(j);
@@ -282,40 +313,6 @@ private:
             done_cv_.notify_all();
             cv_.notify_all();
         }
-    }
-
-    // Requests that may share one packed job: the same method and the same job
-    // options (every field of hfx_options the packed job is built with), so
-    // that each member is computed exactly as it would be alone.
-    static bool same_job_options(const ServerJob& a, const ServerJob& b)
-    {
-        return a.method == b.method && a.precision == b.precision && a.fp32_threshold == b.fp32_threshold &&
-               a.scf.screening_threshold == b.scf.screening_threshold;
-    }
-
-    // Reserve without waiting: false when the footprint does not fit now.
-    bool try_reserve(ServerJob& j, size_t bytes)
-    {
-        std::lock_guard<std::mutex> lk(mu_);
-        if (bytes > budget_) throw Error(HFX_ERR_OOM, "estimated device footprint exceeds the server's HBM budget");
-        if (in_use_ + bytes > budget_) return false;
-        in_use_ += bytes;
-        j.footprint = bytes;
-        return true;
-    }
-
-    // A pack member that must wait for memory goes back to the head of the
-    // queue instead: the memory it waits for may be held by its own pack.
-    void requeue(const std::shared_ptr<ServerJob>& j)
-    {
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            j->state = HFX_JOB_QUEUED;
-            j->t_admit = 0.0;
-            --running_;
-            queue_.push_front(j);
-        }
-        cv_.notify_one();
     }
 
     // reserve the job's footprint, waiting (bounded by the job's timeout) for
@@ -336,96 +333,43 @@ private:
         j.footprint = bytes;
     }
 
-    // a job of a pack ends: result (or failure), budget and slot released
-    void finish_packed(ServerJob& j, ScfOutput* out, hfx_status st, const std::string& msg)
+    // Size class of a job for session grouping: a small job does not wait
+    // each cycle on the O(K^3) steps of a large one.
+    static int size_class(int K) { return K < 100 ? 0 : (K < 300 ? 1 : 2); }
+
+    // The session a packed-mode job joins: one with the same method, options
+    // and size class that has room, else a new one.  Joining happens under
+    // the server lock, so a session found here is not dropped meanwhile.
+    std::shared_ptr<FockSession> join_session(const ServerJob& j, Job& job, int nspin, int* slot)
     {
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            if (out) {
-                j.E_tot = out->E_tot;
-                j.iterations = out->iterations;
-                j.converged = out->converged;
-                j.fock_ms = out->fock_ms;
-                j.fock_builds = out->fock_builds;
-                j.Pa = std::move(out->P);
-                j.Pb = std::move(out->P2);
-                j.status = st;
-                j.state = HFX_JOB_DONE;
-            } else {
-                j.status = st;
-                j.message = msg;
-                j.state = HFX_JOB_FAILED;
+        std::lock_guard<std::mutex> lk(mu_);
+        auto key = std::make_tuple(j.method, j.precision, j.fp32_threshold, job.screening_threshold(),
+                                   size_class(job.K()));
+        auto& list = sessions_[key];
+        for (auto& s : list)
+            if (!s->failed() && s->members() < opt_.pack_max) {
+                *slot = s->join(job);
+                max_session_members_ = std::max(max_session_members_, s->members());
+                return s;
             }
-            --running_;
-            in_use_ -= j.footprint;
-            j.footprint = 0;
-            j.t_end = now_s();
-        }
-        done_cv_.notify_all();
-        cv_.notify_all();
+        auto s = std::make_shared<FockSession>(opt_.device, nspin, job.screening_threshold());
+        *slot = s->join(job);
+        list.push_back(s);
+        ++sessions_created_;
+        max_session_members_ = std::max(max_session_members_, 1);
+        return s;
     }
 
-    void run_pack(const std::vector<std::shared_ptr<ServerJob>>& pack)
+    // A member's SCF ended: leave, and drop the session once it is empty
+    // (a job that joined it meanwhile keeps it alive through its own handle).
+    void leave_session(const std::shared_ptr<FockSession>& s, int slot)
     {
-        std::vector<std::shared_ptr<ServerJob>> live;
-        std::vector<Basis> bases;
-        for (auto& j : pack) {
-            try {
-                if (j->inject_fault == HFX_FAULT_SETUP) throw Error(HFX_ERR_INVALID, "injected fault during setup");
-                std::vector<const char*> syms;
-                for (auto& s : j->symbols) syms.push_back(s.c_str());
-                hfx_molecule mol{(int)syms.size(), syms.data(), j->xyz.data(), j->basis_set.c_str(),
-                                 j->basis_path.empty() ? nullptr : j->basis_path.c_str()};
-                Basis b = build_basis(mol);
-                j->K = b.K;
-                size_t fp = estimate_footprint(b);
-                if (j->inject_fault == HFX_FAULT_OOM) fp = budget_ + 1;
-                if (live.empty()) {
-                    reserve(*j, fp);
-                } else if (!try_reserve(*j, fp)) {
-                    requeue(j);
-                    continue;
-                }
-                if (j->inject_fault == HFX_FAULT_ALLOC) throw Error(HFX_ERR_OOM, "injected allocation failure");
-                bases.push_back(std::move(b));
-                live.push_back(j);
-            } catch (const Error& e) {
-                finish_packed(*j, nullptr, e.code, e.what());
-            } catch (const std::exception& e) {
-                finish_packed(*j, nullptr, HFX_ERR_INVALID, e.what());
-            }
-        }
-        if (live.empty()) return;
-        const ServerJob& first = *live[0];
-        hfx_options o{};
-        o.screening_threshold = first.scf.screening_threshold;
-        o.precision = first.precision;
-        o.fp32_threshold = first.fp32_threshold;
-        o.device = opt_.device;
-        std::vector<ScfControl> ctl(live.size());
-        std::vector<PackedMember> members(live.size());
-        for (size_t i = 0; i < live.size(); ++i) {
-            ServerJob& j = *live[i];
-            ctl[i] = ScfControl{&j.cancel, j.timeout_s > 0 ? j.t_submit + j.timeout_s : 0.0,
-                                j.inject_fault == HFX_FAULT_ITERATION ? 3 : 0};
-            members[i].scf = j.scf;
-            members[i].n_alpha = j.n_alpha;
-            members[i].n_beta = j.n_beta;
-            members[i].ctl = &ctl[i];
-        }
-        std::vector<char> ended(live.size(), 0);
-        try {
-            run_packed(bases, o, first.method == 1 ? 2 : 1, members, 0,
-                       [&](int i, ScfOutput* out, hfx_status st, const std::string& m) {
-                           ended[i] = 1;
-                           finish_packed(*live[i], out, st, m);
-                       });
-        } catch (const Error& e) {
-            for (size_t i = 0; i < live.size(); ++i)
-                if (!ended[i]) finish_packed(*live[i], nullptr, e.code, e.what());
-        } catch (const std::exception& e) {
-            for (size_t i = 0; i < live.size(); ++i)
-                if (!ended[i]) finish_packed(*live[i], nullptr, HFX_ERR_CUDA, e.what());
+        s->leave(slot);
+        std::lock_guard<std::mutex> lk(mu_);
+        if (s->members() > 0) return;
+        for (auto& kv : sessions_) {
+            auto& list = kv.second;
+            list.erase(std::remove(list.begin(), list.end(), s), list.end());
         }
     }
 
@@ -450,10 +394,28 @@ private:
             o.device = opt_.device;
             Job job(b, o);
             ScfSetup setup = scf_setup(b, true);
-            DeviceScf d(job, setup, j->method == 1 ? 2 : 1);
+            const int nspin = j->method == 1 ? 2 : 1;
             const double deadline = j->timeout_s > 0 ? j->t_submit + j->timeout_s : 0.0;
             ScfControl ctl{&j->cancel, deadline, j->inject_fault == HFX_FAULT_ITERATION ? 3 : 0};
-            ScfOutput out = d.run(b, setup, j->scf, j->n_alpha, j->n_beta, nullptr, nullptr, 1e-12, &ctl);
+            ScfOutput out;
+            if (opt_.pack_max > 1) {
+                // packed mode: the job's builds run inside a shared Fock session
+                SessionMember member(job);
+                DeviceScf d(member, setup, nspin);
+                int slot = -1;
+                std::shared_ptr<FockSession> sess = join_session(*j, job, nspin, &slot);
+                member.attach(sess.get(), slot);
+                try {
+                    out = d.run(b, setup, j->scf, j->n_alpha, j->n_beta, nullptr, nullptr, 1e-12, &ctl);
+                } catch (...) {
+                    leave_session(sess, slot);
+                    throw;
+                }
+                leave_session(sess, slot);
+            } else {
+                DeviceScf d(job, setup, nspin);
+                out = d.run(b, setup, j->scf, j->n_alpha, j->n_beta, nullptr, nullptr, 1e-12, &ctl);
+            }
             std::lock_guard<std::mutex> lk(mu_);
             j->E_tot = out.E_tot;
             j->iterations = out.iterations;
@@ -483,9 +445,11 @@ private:
     std::condition_variable cv_, done_cv_;
     std::deque<std::shared_ptr<ServerJob>> queue_;
     std::map<long long, std::shared_ptr<ServerJob>> jobs_;
+    std::map<std::tuple<int, int, double, double, int>, std::vector<std::shared_ptr<FockSession>>> sessions_;
     std::vector<std::thread> workers_;
     long long next_id_ = 1;
     int running_ = 0, max_concurrent_ = 0;
+    int max_session_members_ = 0, sessions_created_ = 0;
     bool stop_ = false;
 };
 

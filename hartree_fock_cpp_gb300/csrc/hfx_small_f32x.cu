@@ -12,7 +12,6 @@ cudaError_t small_spec_f32x(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
     case 2 * 16 + 2: return small_spec<float, 1, 1, 1, 1>(nk, ntasks, s);   // (pp|pp)
     case 3 * 16 + 2: return small_spec<float, 2, 0, 1, 1>(nk, ntasks, s);   // (ds|pp)
     case 4 * 16 + 1: return small_spec<float, 2, 1, 1, 0>(nk, ntasks, s);   // (dp|ps)
-    case 4 * 16 + 3: return small_spec<float, 2, 1, 2, 0>(nk, ntasks, s);   // (dp|ds)
     default: return cudaErrorInvalidValue;
     }
 }

@@ -15,9 +15,11 @@ FAULTS = {"none": 0, "setup": 1, "oom": 2, "alloc": 3, "iteration": 4}
 class Server:
     def __init__(self, max_active=8, hbm_budget_gb=0.0, device=0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
                  pack_max=0):
-        """pack_max > 1: each worker admits up to pack_max queued requests of one
-        method and precision together and runs them in lockstep on one packed
-        job (one Fock build per SCF cycle for the whole pack)."""
+        """pack_max > 1: packed mode.  Each running request joins a Fock session
+        shared with up to pack_max - 1 other requests of the same method,
+        options and size class; every SCF cycle is one build over all of them
+        (one launch per quartet class), and requests that arrive while a
+        session iterates join it at their next cycle."""
         o = _lib.ServerOptions()
         o.max_active = max_active
         o.pack_max = pack_max

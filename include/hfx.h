@@ -306,9 +306,12 @@ typedef struct {
     int device;
     int precision;           /* default precision of requests (HFX_PREC_*) */
     double fp32_threshold;   /* default mixed-precision cut */
-    int pack_max;            /* > 1: a worker admits up to pack_max queued requests of one method and
-                                precision together and runs them in lockstep on one packed job (one
-                                Fock build per SCF cycle for all of them); 0 or 1: one job per worker */
+    int pack_max;            /* > 1: packed mode -- each running request joins a Fock session shared
+                                with up to pack_max - 1 other requests of the same method, options and
+                                size class (K < 100, < 300, larger): every SCF cycle is one build over
+                                all of them, one launch per quartet class, and requests that arrive while
+                                a session iterates join it at their next cycle; 0 or 1: each request
+                                builds on its own streams */
     int reserved[7];
 } hfx_server_options;
 
@@ -342,7 +345,9 @@ typedef struct {
 typedef struct {
     int queued, running, done, failed, max_concurrent;
     double budget_bytes, in_use_bytes;
-    int reserved[6];
+    int max_session_members;   /* packed mode: most jobs one Fock session held at once */
+    int sessions_created;      /* packed mode: Fock sessions opened so far */
+    int reserved[4];
 } hfx_server_stats_t;
 
 hfx_status hfx_server_create(const hfx_server_options *opt, hfx_server **server);

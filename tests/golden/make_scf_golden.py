@@ -28,8 +28,10 @@ tensors):
 Usage (from the repository root; the reference checkout is given by
 HF_REFERENCE):
   HF_REFERENCE=<checkout> python tests/golden/make_scf_golden.py [case ...]
-Cases: water_tz, nacl_tz, benzene, decane (default: all).  Each case merges
-its entries into the existing fixture files.
+Cases: water_tz, nacl_tz, benzene, decane, then water_tz_stable and
+nacl_tz_stable (the same scan points over the stable-Boys tensor; they add
+E_tot_stable / iterations_stable to the existing entries).  Default: all.
+Each case merges its entries into the existing fixture files.
 """
 import importlib.util
 import json
@@ -155,7 +157,37 @@ def case_decane():
     return {"decane_631gs": entry(cfg, "6-31G*", BENCH, res)}, {}
 
 
-CASES = {"water_tz": case_water_tz, "nacl_tz": case_nacl_tz, "benzene": case_benzene, "decane": case_decane}
+def stable_scan(name, configs, points, basis):
+    """The scan points' SCF over the stable-Boys tensor (the reference's
+    algorithm with an accurate F_m(T)): E_tot_stable / iterations_stable
+    beside the reference's own numbers.  Where the reference's upward Boys
+    recursion moves the ERIs far enough to shift the energy by more than
+    1 uHa, the engine (accurate Boys) is held to these."""
+    data = json.load(open(JSON))
+    dens = {}
+    for idx in points:
+        cfg = configs[idx]
+        eri = stable_tensor(cfg, basis)
+        key = "%s_%d" % (name, idx)
+        res = rhf(cfg, basis, eri, SCAN)
+        data[key].update(E_tot_stable=res["E_tot"], iterations_stable=res["iterations"])
+        dens[idx] = res["density"]
+        if key + "_warm" in data and idx - 1 in dens:
+            w = rhf(cfg, basis, eri, SCAN, P0=dens[idx - 1])
+            data[key + "_warm"].update(E_tot_stable=w["E_tot"], iterations_stable=w["iterations"])
+    return data
+
+
+def case_nacl_tz_stable():
+    return stable_scan("nacl_ccpvtz", W.nacl_scan(64), NACL_POINTS, "cc-pVTZ"), {}
+
+
+def case_water_tz_stable():
+    return stable_scan("water_ccpvtz", W.water_scan(64), WATER_POINTS, "cc-pVTZ"), {}
+
+
+CASES = {"water_tz": case_water_tz, "nacl_tz": case_nacl_tz, "benzene": case_benzene, "decane": case_decane,
+         "water_tz_stable": case_water_tz_stable, "nacl_tz_stable": case_nacl_tz_stable}
 
 
 def main(names):

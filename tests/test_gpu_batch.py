@@ -89,7 +89,8 @@ def test_batch_warm_chain_matches_reference_loop_fixture():
     head, warm = g["water_ccpvtz_20"], g["water_ccpvtz_21_warm"]
     cfg = lambda c: [(s, tuple(x)) for s, x in c["config"]]
     res, _ = H.batch_scf([(cfg(head), "cc-pVTZ"), (cfg(warm), "cc-pVTZ")], warm_chain=2)
-    assert abs(res[0]["E_tot"] - head["E_tot"]) < E_TOL
-    assert abs(res[0]["iterations"] - head["iterations"]) <= 1
-    assert abs(res[1]["E_tot"] - warm["E_tot"]) < E_TOL
-    assert abs(res[1]["iterations"] - warm["iterations"]) <= 1, (res[1]["iterations"], warm["iterations"])
+    for r, c in ((res[0], head), (res[1], warm)):
+        # the reference loop over the accurate-Boys tensor where the fixture has it
+        E, it = c.get("E_tot_stable", c["E_tot"]), c.get("iterations_stable", c["iterations"])
+        assert abs(r["E_tot"] - E) < E_TOL
+        assert abs(r["iterations"] - it) <= 1, (r["iterations"], it)

@@ -7,13 +7,17 @@ reference's own integral code and the oracle's restatement of its SCF loop
     direct build (hfx_fock_rhf / hfx_fock_uhf, the class and warp kernels),
     against the oracle's stored-tensor contractions (linalg.hpp:100-129,
     215-296) with the accurate Boys function: 1e-10 per element.  Against the
-    reference's own tensor (whose upward Boys recursion moves single ERIs by
-    up to ~1e-8) the bound is 1e-6.
+    reference's own tensor the engine may differ only as much as the
+    accurate-Boys contraction does: the reference's upward Boys recursion
+    (integrals.hpp:223-266) moves G by ~1e-7 on water and ~4e-4 on NaCl.
   * SCF energies and iteration counts of the benchmark configurations
     (benzene/cc-pVDZ, n-decane/6-31G*, NaCl and water cc-pVTZ scan points,
     and warm-started scan points): the engine's device SCF against the
-    reference's rhf_diis (scf.hpp:205-419) over the reference's own tensor:
-    1 uHa and +-1 iteration.
+    reference's rhf_diis (scf.hpp:205-419) over the reference's own tensor,
+    1 uHa and +-1 iteration.  Where the fixture also holds the same loop over
+    the accurate-Boys tensor (E_tot_stable; the NaCl and water scan points),
+    the engine is held to that at 1 uHa / +-1, and to the reference's own
+    number within the reference's Boys error plus 1 uHa.
 """
 import json
 import os
@@ -26,7 +30,6 @@ import hartree_fock_cpp_gb300 as H
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MAT_TOL = 1e-10          # per element, against the stable-Boys oracle
-MAT_TOL_REF = 1e-6       # per element, against the reference's own tensor
 E_TOL = 1e-6             # Eh
 IT_TOL = 1
 
@@ -48,7 +51,8 @@ def test_fock_matrices_match_oracle_fixture(name):
         G = fb.repulsion_matrix(m["P"])
         J, Ka, Kb = fb.coulomb_exchange(m["Pa"], m["Pb"])
     assert np.abs(G - m["G"]).max() < MAT_TOL
-    assert np.abs(G - m["G_ref"]).max() < MAT_TOL_REF
+    boys_err = np.abs(m["G"] - m["G_ref"]).max()
+    assert np.abs(G - m["G_ref"]).max() <= boys_err + MAT_TOL
     assert np.abs(J - m["J"]).max() < MAT_TOL
     assert np.abs(Ka - m["Ka"]).max() < MAT_TOL
     assert np.abs(Kb - m["Kb"]).max() < MAT_TOL
@@ -64,6 +68,17 @@ def _solve(case, P0=None, **kw):
                       set_initial_density=P0 is not None, P0=P0, **kw)
 
 
+def _check_against_reference_loop(r, case):
+    if "E_tot_stable" in case:
+        assert abs(r["E_tot"] - case["E_tot_stable"]) < E_TOL, (r["E_tot"], case["E_tot_stable"])
+        assert abs(r["iterations"] - case["iterations_stable"]) <= IT_TOL, (r["iterations"], case["iterations_stable"])
+        boys_err = abs(case["E_tot_stable"] - case["E_tot"])
+        assert abs(r["E_tot"] - case["E_tot"]) < boys_err + E_TOL
+    else:
+        assert abs(r["E_tot"] - case["E_tot"]) < E_TOL, (r["E_tot"], case["E_tot"])
+        assert abs(r["iterations"] - case["iterations"]) <= IT_TOL, (r["iterations"], case["iterations"])
+
+
 @pytest.mark.parametrize("name", COLD)
 def test_scf_matches_reference_loop(name):
     case = CASES[name]
@@ -71,8 +86,7 @@ def test_scf_matches_reference_loop(name):
     r = _solve(case)
     assert r["converged"]
     assert r["K"] == case["K"]
-    assert abs(r["E_tot"] - case["E_tot"]) < E_TOL, (r["E_tot"], case["E_tot"])
-    assert abs(r["iterations"] - case["iterations"]) <= IT_TOL, (r["iterations"], case["iterations"])
+    _check_against_reference_loop(r, case)
 
 
 @pytest.mark.parametrize("name", WARM)
@@ -83,8 +97,7 @@ def test_warm_started_scan_point_matches_reference_loop(name):
     prev = _solve(CASES[case["warm_start_from"]])
     r = _solve(case, P0=prev["density"])
     assert r["converged"]
-    assert abs(r["E_tot"] - case["E_tot"]) < E_TOL
-    assert abs(r["iterations"] - case["iterations"]) <= IT_TOL, (r["iterations"], case["iterations"])
+    _check_against_reference_loop(r, case)
 
 
 def test_mixed_precision_decane_energy_matches_reference_loop():

@@ -78,18 +78,20 @@ def test_cancel_queued_job():
 
 
 def test_packed_mode_results_same_alone_and_in_the_pack():
-    """pack_max > 1: requests of one method are admitted together and iterate in
-    lockstep on one packed job; each result equals the job run alone, and a
-    faulty request in the pack fails alone."""
+    """pack_max > 1: running requests of one method share Fock sessions (one
+    build per SCF cycle over all members of a size class, one launch per
+    class); each result equals the job run alone, and a faulty request in a
+    session fails alone."""
     rhf = [j for j in MIX if j["method"] == "RHF"]
     alone = [_alone(j) for j in rhf]
-    with Server(max_active=2, pack_max=8) as srv:
+    with Server(max_active=8, pack_max=8) as srv:
         ids = [srv.submit(**j) for j in rhf]
         bad = srv.submit(config=W.water(), basis_set="6-31G*", inject_fault="iteration")
         uhf = srv.submit(config=OH, basis_set="6-31G*", method="UHF", spin=(5, 4))
         srv.drain(600)
         infos = [srv.poll(i) for i in ids]
         ib, iu = srv.poll(bad), srv.poll(uhf)
+        st = srv.stats()
     for j, a, inf in zip(rhf, alone, infos):
         assert inf["state"] == "done", inf
         assert inf["converged"]
@@ -97,28 +99,55 @@ def test_packed_mode_results_same_alone_and_in_the_pack():
         assert abs(inf["iterations"] - a["iterations"]) <= 1
     assert ib["state"] == "failed"
     assert iu["state"] == "done" and iu["converged"]
+    assert st["max_session_members"] >= 2
+
+
+def test_request_arriving_mid_scf_joins_the_running_session():
+    """A request submitted while another of its size class iterates joins
+    that session at its next cycle (continuous batching inside one build);
+    both results equal the jobs run alone.  Mixed precision, where a cycle can
+    hold mixed and FP64 (incremental) builds as separate variants."""
+    import time
+    jobs = [dict(config=W.n_decane(), basis_set="6-31G*"), dict(config=W.benzene(), basis_set="cc-pVDZ")]
+    kw = dict(precision=H.HFX_PREC_MIXED, fp32_threshold=0.03)
+    alone = [H.rhf_diis(j["config"], j["basis_set"], **kw) for j in jobs]
+    with Server(max_active=4, pack_max=4, precision=H.HFX_PREC_MIXED, fp32_threshold=0.03) as srv:
+        first = srv.submit(**jobs[0])
+        time.sleep(0.3)
+        second = srv.submit(**jobs[1])
+        srv.drain(600)
+        infos = [srv.poll(first), srv.poll(second)]
+        st = srv.stats()
+    for a, inf in zip(alone, infos):
+        assert inf["state"] == "done" and inf["converged"], inf
+        assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL
+        assert abs(inf["iterations"] - a["iterations"]) <= 1
+    assert infos[1]["t_admit"] < infos[0]["t_end"]       # admitted while the first was iterating
+    assert st["max_session_members"] == 2 and st["sessions_created"] == 1
 
 
 def test_packed_members_keep_their_own_screening_threshold():
-    """Requests with different Schwarz thresholds never share a packed job:
+    """Requests with different Schwarz thresholds never share a Fock session:
     each result equals the same request run alone."""
     thr = (1e-8, 1e-3)
     alone = [H.rhf_diis(W.water(), "cc-pVDZ", screening_threshold=t) for t in thr]
     assert abs(alone[0]["E_tot"] - alone[1]["E_tot"]) > 10 * E_TOL   # the thresholds matter
-    with Server(max_active=1, pack_max=4) as srv:
+    with Server(max_active=2, pack_max=4) as srv:
         ids = [srv.submit(W.water(), "cc-pVDZ", screening_threshold=t) for t in thr]
         srv.drain(300)
         infos = [srv.poll(i) for i in ids]
+        st = srv.stats()
     for a, inf in zip(alone, infos):
         assert inf["state"] == "done" and inf["converged"], inf
         assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL
+    assert st["sessions_created"] == 2
 
 
-def test_packed_admission_never_waits_on_its_own_pack():
-    """The budget fits one request but not two: the pack runs the member that
-    fits and requeues the others instead of waiting for memory that only the
-    pack itself would release."""
-    with Server(max_active=1, pack_max=4, hbm_budget_gb=0.1) as srv:
+def test_packed_admission_within_a_small_memory_budget():
+    """The budget fits one request but not two: the second waits for memory
+    outside any session (a session never waits on a request that has not
+    joined it), and both finish."""
+    with Server(max_active=2, pack_max=4, hbm_budget_gb=0.1) as srv:
         ids = [srv.submit(W.water(), "STO-3G") for _ in range(3)]
         srv.drain(120)
         infos = [srv.poll(i) for i in ids]
