@@ -218,24 +218,19 @@ __device__ __forceinline__ long long spidx(int a, int b)
 // the bra transform).
 constexpr int kAmortizeBytes = 256;
 
-template <typename T, int LA, int LB, int LC, int LD, int NK>
-__global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
+// One task's ket component pairs cd in [C0, C1): primitive integrals, their
+// contraction into acc[ab][cd - C0], and the digestion of that block.
+template <typename T, int LA, int LB, int LC, int LD, int NK, int C0, int C1>
+__device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task& tk, const DPair& bra,
+                                              const DPair& ket)
 {
     constexpr int L1 = LA + LB, L2 = LC + LD, L = L1 + L2;
     constexpr int NB = c_nc(LB), ND = c_nc(LD);
-    constexpr int NAB = c_nc(LA) * NB, NCD = c_nc(LC) * ND;
+    constexpr int NAB = c_nc(LA) * NB, NCD = C1 - C0;
     constexpr int H1 = c_nh(L1), HL = c_nh(L);
     constexpr int SB = rec_stride(LA, LB), SK = rec_stride(LC, LD);
     // amortised bra transform when the ket sum fits in registers beside acc
     constexpr bool AMB = NCD * H1 * (int)sizeof(T) <= kAmortizeBytes;
-
-    const int task = blockIdx.x * blockDim.x + threadIdx.x;
-    if (task >= a.ntasks) return;
-    const Task tk = a.tasks[task];
-    const DPair bra = a.pairs[tk.bra];
-    const DPair ket = a.pairs[tk.ket];
-    if (molecule_inactive(bra, a.active)) return;
-    if (density_negligible(bra, ket, a.Dsh, a.dthr)) return;
 
     T acc[NAB][NCD];
 #pragma unroll
@@ -288,11 +283,11 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             T R[HL];
             hermite_R<T, L>(X, Y, Z, sd, R);
             cfor<0, NCD>([&](auto cdc) {
-                constexpr int cd = decltype(cdc)::value;
-                constexpr int c = cd / ND, d = cd % ND;
+                constexpr int cd = decltype(cdc)::value;       // local index in the block
+                constexpr int c = (C0 + cd) / ND, d = (C0 + cd) % ND;
                 constexpr int nx = comp_x(LC, c) + comp_x(LD, d), ny = comp_y(LC, c) + comp_y(LD, d),
                               nz = comp_z(LC, c) + comp_z(LD, d);
-                constexpr int k0 = coef_off(LC, LD, cd);
+                constexpr int k0 = coef_off(LC, LD, C0 + cd);
                 T W[AMB ? 1 : H1];
                 if constexpr (!AMB) {
 #pragma unroll
@@ -379,7 +374,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             if (bra.same && ia < ib) continue;
 #pragma unroll
             for (int cd = 0; cd < NCD; ++cd) {
-                const int ic = cd / ND, id = cd % ND;
+                const int ic = (C0 + cd) / ND, id = (C0 + cd) % ND;
                 const int k = ket.bf0 + ic, l = ket.bf1 + id;
                 if (ket.same && ic < id) continue;
                 const long long pkl = spidx(k, l);
@@ -417,7 +412,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             const double qb = __ldg(Qbf + pij);
 #pragma unroll
             for (int cd = 0; cd < NCD; ++cd) {
-                const int ic = cd / ND, id = cd % ND;
+                const int ic = (C0 + cd) / ND, id = (C0 + cd) % ND;
                 const int k = ket.bf0 + ic, l = ket.bf1 + id;
                 const long long pkl = spidx(k, l);
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) || (same_pair && pij < pkl) ||
@@ -436,7 +431,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
         for (int ab = 0; ab < NAB; ++ab) {
             T sj = 0;
 #pragma unroll
-            for (int cd = 0; cd < NCD; ++cd) sj += d32(Dj32, k0 + cd / ND, l0 + cd % ND) * acc[ab][cd];
+            for (int cd = 0; cd < NCD; ++cd) sj += d32(Dj32, k0 + (C0 + cd) / ND, l0 + (C0 + cd) % ND) * acc[ab][cd];
             put(J, i0 + ab / NB, j0 + ab % NB, sj);
         }
 #pragma unroll
@@ -444,7 +439,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
             T sj = 0;
 #pragma unroll
             for (int ab = 0; ab < NAB; ++ab) sj += d32(Dj32, i0 + ab / NB, j0 + ab % NB) * acc[ab][cd];
-            put(J, k0 + cd / ND, l0 + cd % ND, sj);
+            put(J, k0 + (C0 + cd) / ND, l0 + (C0 + cd) % ND, sj);
         }
 #pragma unroll
         for (int sp = 0; sp < NK; ++sp) {
@@ -461,7 +456,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
                     for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                         for (int id = 0; id < ND; ++id)
-                            s += d32(Dk32, j0 + ib, l0 + id) * acc[ia * NB + ib][ic * ND + id];
+                            if (ic * ND + id >= C0 && ic * ND + id < C1) s += d32(Dk32, j0 + ib, l0 + id) * acc[ia * NB + ib][ic * ND + id - C0];
                     put(KK, i0 + ia, k0 + ic, s);
                 }
 #pragma unroll
@@ -473,7 +468,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
                     for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                         for (int ic = 0; ic < NC; ++ic)
-                            s += d32(Dk32, i0 + ia, k0 + ic) * acc[ia * NB + ib][ic * ND + id];
+                            if (ic * ND + id >= C0 && ic * ND + id < C1) s += d32(Dk32, i0 + ia, k0 + ic) * acc[ia * NB + ib][ic * ND + id - C0];
                     put(KK, j0 + ib, l0 + id, s);
                 }
 #pragma unroll
@@ -485,7 +480,7 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
                     for (int ib = 0; ib < NB; ++ib)
 #pragma unroll
                         for (int ic = 0; ic < NC; ++ic)
-                            s += d32(Dk32, j0 + ib, k0 + ic) * acc[ia * NB + ib][ic * ND + id];
+                            if (ic * ND + id >= C0 && ic * ND + id < C1) s += d32(Dk32, j0 + ib, k0 + ic) * acc[ia * NB + ib][ic * ND + id - C0];
                     put(KK, i0 + ia, l0 + id, s);
                 }
 #pragma unroll
@@ -497,10 +492,51 @@ __global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
                     for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
                         for (int id = 0; id < ND; ++id)
-                            s += d32(Dk32, i0 + ia, l0 + id) * acc[ia * NB + ib][ic * ND + id];
+                            if (ic * ND + id >= C0 && ic * ND + id < C1) s += d32(Dk32, i0 + ia, l0 + id) * acc[ia * NB + ib][ic * ND + id - C0];
                     put(KK, j0 + ib, k0 + ic, s);
                 }
         }
+    }
+}
+
+// Ket component-pair blocks of a class kernel: float classes whose
+// accumulators would not fit the register file split their ket component
+// pairs over small_ncb(...) threads per task (each computes R, its block's
+// ket sums, its block's integrals and their digestion; J and K are linear in
+// the integrals), at most ~40 accumulators per thread.
+template <typename T, int LA, int LB, int LC, int LD>
+__host__ __device__ constexpr int small_ncb()
+{
+    constexpr int ncd = c_nc(LC) * c_nc(LD);
+    if constexpr (sizeof(T) == 8) {
+        return 1;
+    } else {
+        constexpr int nab = c_nc(LA) * c_nc(LB);
+        int nb = 1;
+        while (nb < ncd && nab * ((ncd + nb - 1) / nb) > 40) ++nb;
+        return nb;
+    }
+}
+
+template <typename T, int LA, int LB, int LC, int LD, int NK>
+__global__ void __launch_bounds__(128) k_small(SmallArgs<T> a)
+{
+    constexpr int NCD = c_nc(LC) * c_nc(LD);
+    constexpr int NCB = small_ncb<T, LA, LB, LC, LD>();
+    const int task = blockIdx.x * blockDim.x + threadIdx.x;
+    if (task >= a.ntasks) return;
+    const Task tk = a.tasks[task];
+    const DPair bra = a.pairs[tk.bra];
+    const DPair ket = a.pairs[tk.ket];
+    if (molecule_inactive(bra, a.active)) return;
+    if (density_negligible(bra, ket, a.Dsh, a.dthr)) return;
+    if constexpr (NCB == 1) {
+        small_quartet<T, LA, LB, LC, LD, NK, 0, NCD>(a, tk, bra, ket);
+    } else {
+        cfor<0, NCB>([&](auto bc) {
+            constexpr int b = decltype(bc)::value;
+            if (blockIdx.y == b) small_quartet<T, LA, LB, LC, LD, NK, b * NCD / NCB, (b + 1) * NCD / NCB>(a, tk, bra, ket);
+        });
     }
 }
 
@@ -510,7 +546,7 @@ cudaError_t small_spec(int nk, int ntasks, KernelSpec* s)
 {
     s->func = nk == 2 ? (const void*)k_small<T, LA, LB, LC, LD, 2> : (const void*)k_small<T, LA, LB, LC, LD, 1>;
     s->block = dim3(128);
-    s->grid = dim3((unsigned)((ntasks + 127) / 128));
+    s->grid = dim3((unsigned)((ntasks + 127) / 128), (unsigned)small_ncb<T, LA, LB, LC, LD>());
     s->smem = 0;
     return cudaSuccess;
 }

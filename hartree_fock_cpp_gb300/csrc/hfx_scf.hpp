@@ -19,6 +19,31 @@ using GBuilder = std::function<void(const double* P, double* G, int mode)>;
 // UHF builder: (Pa, Pb) -> J[Pa+Pb], K[Pa], K[Pb].
 using JKBuilder = std::function<void(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, int mode)>;
 
+// When the mixed-precision SCF leaves its FP32 phase: once RMSD(P) is
+// within a few epsilon of convergence (the last cycles then run as FP64
+// builds -- one full, then FP64 builds of the density change), or earlier
+// if the mixed-precision iterations stop making progress (RMSD not down by
+// a third over three iterations), which is where the FP32 quartets' error
+// would hold the SCF back.
+class MixedPhaseSwitch {
+public:
+    explicit MixedPhaseSwitch(double epsilon) : tol_(kSwitchFactor * epsilon) {}
+    // true once the FP32 phase should end; call once per iteration
+    bool update(double rmsd)
+    {
+        hist_.push_back(rmsd);
+        const size_t n = hist_.size();
+        if (rmsd < tol_) return true;
+        return n >= 4 && rmsd > kStallRatio * hist_[n - 4];
+    }
+    static constexpr double kSwitchFactor = 2.0;
+    static constexpr double kStallRatio = 2.0 / 3.0;
+
+private:
+    double tol_;
+    std::vector<double> hist_;
+};
+
 struct ScfOutput {
     double E_tot = 0, E_ele = 0, E_nuc = 0, E_prev = 0, last_rmsd = 0;
     int iterations = 0;

@@ -1,10 +1,14 @@
-// hfx_small_f32x.cu -- float-only small-class kernels for the larger classes
-// whose thread-per-quartet form fits the register file in FP32 (in FP64
-// these classes run on the warp kernel).  Split from hfx_small_f32.cu so the
-// two translation units compile in parallel.
+// hfx_small_f32x.cu -- float-only class kernels for the larger classes whose
+// thread-per-quartet form fits the register file in FP32 once their ket
+// component pairs are split over a few threads per task (in FP64 these
+// classes run on the warp kernel).  Split from hfx_small_f32.cu (and the d-d
+// classes into hfx_small_f32y/z/w.cu) so the translation units compile in
+// parallel.
 #include "hfx_class.cuh"
 
 namespace hfx {
+
+cudaError_t small_spec_f32y(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // hfx_small_f32y.cu
 
 cudaError_t small_spec_f32x(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
 {
@@ -12,7 +16,9 @@ cudaError_t small_spec_f32x(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
     case 2 * 16 + 2: return small_spec<float, 1, 1, 1, 1>(nk, ntasks, s);   // (pp|pp)
     case 3 * 16 + 2: return small_spec<float, 2, 0, 1, 1>(nk, ntasks, s);   // (ds|pp)
     case 4 * 16 + 1: return small_spec<float, 2, 1, 1, 0>(nk, ntasks, s);   // (dp|ps)
-    default: return cudaErrorInvalidValue;
+    case 4 * 16 + 2: return small_spec<float, 2, 1, 1, 1>(nk, ntasks, s);   // (dp|pp)
+    case 4 * 16 + 3: return small_spec<float, 2, 1, 2, 0>(nk, ntasks, s);   // (dp|ds)
+    default: return small_spec_f32y(pcb, pck, nk, ntasks, s);
     }
 }
 

@@ -31,7 +31,9 @@ HF_REFERENCE):
 Cases: water_tz, nacl_tz, benzene, decane, then water_tz_stable and
 nacl_tz_stable (the same scan points over the stable-Boys tensor; they add
 E_tot_stable / iterations_stable to the existing entries).  Default: all.
-Each case merges its entries into the existing fixture files.
+Each case merges its entries into the existing fixture files.  With
+HF_TENSOR_CACHE=<directory> the tensors are kept there between runs (the
+stable-Boys stages reuse the tensors of the earlier ones).
 """
 import importlib.util
 import json
@@ -66,21 +68,42 @@ def log(msg):
     print("[%s] %s" % (time.strftime("%H:%M:%S"), msg), flush=True)
 
 
-def ref_tensor(config, basis):
-    r = O.RefLib()
-    K = r.build(config, basis, O.BASIS_PATH)
-    t = time.perf_counter()
-    eri = r.repulsion_tensor_mt(1e-8)
-    log("reference tensor %s K=%d: %d unique ERIs in %.0f s" % (basis, K, eri.size, time.perf_counter() - t))
+CACHE = os.environ.get("HF_TENSOR_CACHE")   # optional directory: tensors kept between runs
+
+
+def _cached(kind, config, basis, make):
+    if not CACHE:
+        return make()
+    import hashlib
+    key = hashlib.sha1(json.dumps([kind, basis, config]).encode()).hexdigest()[:16]
+    path = os.path.join(CACHE, "%s_%s.npy" % (kind, key))
+    if os.path.exists(path):
+        return np.load(path)
+    eri = make()
+    os.makedirs(CACHE, exist_ok=True)
+    np.save(path, eri)
     return eri
+
+
+def ref_tensor(config, basis):
+    def make():
+        r = O.RefLib()
+        K = r.build(config, basis, O.BASIS_PATH)
+        t = time.perf_counter()
+        eri = r.repulsion_tensor_mt(1e-8)
+        log("reference tensor %s K=%d: %d unique ERIs in %.0f s" % (basis, K, eri.size, time.perf_counter() - t))
+        return eri
+    return _cached("ref", config, basis, make)
 
 
 def stable_tensor(config, basis):
-    orc = O.Oracle(config, basis, stable_boys=True)
-    t = time.perf_counter()
-    eri = orc.repulsion_tensor_mt(1e-8)
-    log("stable-Boys tensor %s K=%d in %.0f s" % (basis, orc.K, time.perf_counter() - t))
-    return eri
+    def make():
+        orc = O.Oracle(config, basis, stable_boys=True)
+        t = time.perf_counter()
+        eri = orc.repulsion_tensor_mt(1e-8)
+        log("stable-Boys tensor %s K=%d in %.0f s" % (basis, orc.K, time.perf_counter() - t))
+        return eri
+    return _cached("stable", config, basis, make)
 
 
 def rhf(config, basis, eri, settings, P0=None):
