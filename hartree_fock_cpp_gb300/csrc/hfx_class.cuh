@@ -404,19 +404,22 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
         // added to the FP64 accumulators once -- nab + ncd + na nc + na nd +
         // nb nc + nb nd atomics per quartet instead of 6 per integral.
         constexpr int NA = c_nc(LA), NC = c_nc(LC);
+        const T* __restrict__ QbT = schwarz_of<T>(a) + bra.qoff;
+        const bool screen = a.thr >= 0.0;
+        const T thrT = (T)a.thr;
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) {
             const int ia = ab / NB, ib = ab % NB;
             const int i = bra.bf0 + ia, j = bra.bf1 + ib;
             const long long pij = spidx(i, j);
-            const double qb = __ldg(Qbf + pij);
+            const T qb = __ldg(QbT + pij);
 #pragma unroll
             for (int cd = 0; cd < NCD; ++cd) {
                 const int ic = (C0 + cd) / ND, id = (C0 + cd) % ND;
                 const int k = ket.bf0 + ic, l = ket.bf1 + id;
                 const long long pkl = spidx(k, l);
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) || (same_pair && pij < pkl) ||
-                                  (a.thr >= 0.0 && qb * __ldg(Qbf + pkl) < a.thr);
+                                  (screen && qb * __ldg(QbT + pkl) < thrT);
                 const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
                 acc[ab][cd] = skip ? (T)0 : acc[ab][cd] * f;
             }

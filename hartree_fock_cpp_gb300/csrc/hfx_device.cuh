@@ -169,6 +169,9 @@ struct SmallArgs {
     const float* Dj32;
     const float* Dk32;
     const float* Dk232;
+    // FP32 kernels: float copy of the BF-pair Schwarz bounds (the digestion's
+    // screen then needs no FP64 arithmetic); addressed with bra.qoff
+    const float* Qbf32;
 };
 
 // Arguments of the warp-per-shell-quartet kernel.
@@ -204,6 +207,9 @@ struct WarpArgs {
     const float* Dj32;
     const float* Dk32;
     const float* Dk232;
+    // FP32 kernels: float copy of the BF-pair Schwarz bounds (the digestion's
+    // screen then needs no FP64 arithmetic); addressed with bra.qoff
+    const float* Qbf32;
 };
 
 #ifdef __CUDACC__
@@ -236,6 +242,17 @@ __device__ __forceinline__ const T* density_of(const double* d64, const float* d
         return d64;
     else
         return d32;
+}
+
+// The BF-pair Schwarz bounds a kernel of precision T screens with: FP64
+// kernels the double table, FP32 kernels its float copy.
+template <typename T, typename A>
+__device__ __forceinline__ const T* schwarz_of(const A& a)
+{
+    if constexpr (sizeof(T) == 8)
+        return a.Qbf;
+    else
+        return a.Qbf32;
 }
 
 // Quartet of a molecule that takes no part in this build of a packed job.

@@ -215,6 +215,10 @@ void Job::init(const hfx_options& opt)
 
     build_pairs();
     compute_schwarz();
+    {
+        std::vector<float> q32(qbf_.begin(), qbf_.end());
+        d_qbf32_.upload(q32, stream_);
+    }
     // shell-pair Schwarz maxima into the device pair records (density screening)
     for (size_t p = 0; p < dpairs_host_.size(); ++p) dpairs_host_[p].qmax = qsh_[p];
     d_pairs_.upload(dpairs_host_, stream_);
@@ -933,7 +937,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
             if (g.fp32) {
                 SmallArgs<float> a{d_pairs_.p, d_rec32_.p, tasks + g.off, (int)g.n, d_boys32_.p,
                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active,
-                                   Dj32, Dk32, Dk232};
+                                   Dj32, Dk32, Dk232, d_qbf32_.p};
                 cuda_check(small_spec_f32(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
@@ -952,7 +956,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                                   tasks + g.off, (int)g.n, ctr + gi, d_boys32_.p,
                                   opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
                                   g.lane_min_npp,
-                                  Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232};
+                                  Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232, d_qbf32_.p};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             } else {

@@ -339,6 +339,7 @@ private:
     DevBuf<double> d_epool_;
     DevBuf<double> d_boys_;
     DevBuf<double> d_qbf_;
+    DevBuf<float> d_qbf32_;         // float copy of d_qbf_ (the FP32 kernels' screen)
     DevBuf<unsigned long long> d_qsh_;
     DevBuf<Task> d_tasks_;
     int ntasks_ = 0;

@@ -173,6 +173,7 @@ void FockSession::relayout()
         const long long d64 = elem_offset(j.d_rec64_.p, anchor64_.p, sizeof(double));
         const long long d32 = elem_offset(j.d_rec32_.p, anchor32_.p, sizeof(float));
         const long long dq = elem_offset(j.d_qbf_.p, anchor64_.p, sizeof(double));
+        const long long dq32 = elem_offset(j.d_qbf32_.p, anchor32_.p, sizeof(float));
         for (const DPair& src : j.dpairs_host_) {
             DPair x = src;
             x.moff = m.moff;
@@ -184,6 +185,7 @@ void FockSession::relayout()
             DPair a = x, b = x;
             a.rec_off = d64 + src.rec_off;
             b.rec_off = d32 + src.rec_off;
+            b.qoff = dq32 + src.qoff;   // the FP32 kernels screen with the float table
             h64.push_back(a);
             h32.push_back(b);
         }
@@ -365,8 +367,8 @@ void FockSession::launch(int nk, bool mixed_plan, double dthr)
             const int lane = 1 + next_aux;
             next_aux = (next_aux + 1) % naux;
             if (g.fp32) {
-                SmallArgs<float> a{pairs32_.p, anchor32_.p, tasks + g.off, (int)g.n, boys32_.p, thr_, anchor64_.p,
-                                   0, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active, Dj32, Dk32, Dk232};
+                SmallArgs<float> a{pairs32_.p, anchor32_.p, tasks + g.off, (int)g.n, boys32_.p, thr_, nullptr,
+                                   0, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr, active, Dj32, Dk32, Dk232, anchor32_.p};
                 cuda_check(small_spec_f32(g.pcb, g.pck, nk, (int)g.n, &ks), "session small-class kernel");
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
@@ -381,8 +383,8 @@ void FockSession::launch(int nk, bool mixed_plan, double dthr)
             cuda_check(warp_spec(g.fp32, nk, g.grid, g.warps_per_cta, g.slice, &ks), "session warp kernel");
             if (g.fp32) {
                 WarpArgs<float> a{pairs32_.p, anchor32_.p, pct_.p, abs_.p, kh_.p, kl_.p, tasks + g.off, (int)g.n,
-                                  ctr + gi, boys32_.p, thr_, anchor64_.p, 0, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
-                                  g.lane_min_npp, Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232};
+                                  ctr + gi, boys32_.p, thr_, nullptr, 0, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
+                                  g.lane_min_npp, Dsh, dthr, nullptr, nullptr, active, Dj32, Dk32, Dk232, anchor32_.p};
                 void* prm[] = {&a};
                 sk.kernel(0, ks, prm);
             } else {

@@ -439,6 +439,9 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             // products with the float density copies) and adds the sum to the
             // FP64 accumulator: nab + ncd + na nc + na nd + nb nc + nb nd
             // atomics per quartet instead of 6 per integral.
+            const T* __restrict__ QbT = schwarz_of<T>(a) + bra.qoff;
+            const bool screen = a.thr >= 0.0;
+            const T thrT = (T)a.thr;
             for (int e = lane; e < nout; e += 32) {
                 const int ab = e / ncd, cd = e - ab * ncd;
                 const int ia = ab / n1, ib = ab - ia * n1, ic = cd / n3, id = cd - ic * n3;
@@ -446,7 +449,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 const long long pij = wpidx(i, j), pkl = wpidx(k, l);
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) ||
                                   (task.bra == task.ket && pij < pkl) ||
-                                  (a.thr >= 0.0 && __ldg(Qbf + pij) * __ldg(Qbf + pkl) < a.thr);
+                                  (screen && __ldg(QbT + pij) * __ldg(QbT + pkl) < thrT);
                 const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
                 acc[e] = skip ? (T)0 : acc[e] * f;
             }
