@@ -22,26 +22,33 @@ using JKBuilder = std::function<void(const double* Pa, const double* Pb, double*
 // When the mixed-precision SCF leaves its FP32 phase: once RMSD(P) is
 // within a few epsilon of convergence (the last cycles then run as FP64
 // builds -- one full, then FP64 builds of the density change), or earlier
-// if the mixed-precision iterations stop making progress (RMSD not down by
-// a third over three iterations), which is where the FP32 quartets' error
-// would hold the SCF back.
+// if the mixed-precision iterations stop making progress -- no new low of
+// RMSD(P) by at least 10% in four iterations, checked from the eighth
+// iteration on (DIIS is running by then) -- which is where the FP32
+// quartets' error would hold the SCF back.
 class MixedPhaseSwitch {
 public:
     explicit MixedPhaseSwitch(double epsilon) : tol_(kSwitchFactor * epsilon) {}
     // true once the FP32 phase should end; call once per iteration
     bool update(double rmsd)
     {
-        hist_.push_back(rmsd);
-        const size_t n = hist_.size();
+        ++n_;
         if (rmsd < tol_) return true;
-        return n >= 4 && rmsd > kStallRatio * hist_[n - 4];
+        if (rmsd < 0.9 * best_) {
+            best_ = rmsd;
+            since_ = 0;
+        } else {
+            ++since_;
+        }
+        return n_ >= kMinIterations && since_ >= kStallIterations;
     }
     static constexpr double kSwitchFactor = 2.0;
-    static constexpr double kStallRatio = 2.0 / 3.0;
+    static constexpr int kMinIterations = 8, kStallIterations = 4;
 
 private:
     double tol_;
-    std::vector<double> hist_;
+    double best_ = 1e300;
+    int n_ = 0, since_ = 0;
 };
 
 struct ScfOutput {
