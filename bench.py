@@ -314,7 +314,8 @@ def run_engine(args):
                                                           (fp64_peak, fp32_peak))
 
     # ---- served request stream: continuous batching vs one-at-a-time FP64 ----
-    served = section(serve_section, H, W, args.serve_jobs, local) if args.serve_jobs > 0 else None
+    served = section(serve_section, H, W, args.serve_jobs, local, rate_list(args.serve_rates)) \
+        if args.serve_jobs > 0 else None
 
     # ---- batched radial scans: packed lockstep SCF vs one-at-a-time FP64 -----
     scans = section(scan_section, H, W, args.scan_points) if args.scan_points > 0 else None
@@ -607,6 +608,18 @@ def scan_section(H, W, n_each, chain=8):
             "max_abs_dE_vs_single": float(max(dE)), "max_iteration_diff_warm_points": int(max(dI)) if dI else 0}
 
 
+def rate_list(text):
+    return tuple(float(x) for x in text.split(",") if x.strip())
+
+
+def run_serve_only(args):
+    """The served-stream section alone (a longer prefix of the stream, other
+    rates): one JSON object."""
+    import hartree_fock_cpp_gb300 as H
+    from hartree_fock_cpp_gb300 import workloads as W
+    print(json.dumps(serve_section(H, W, args.serve_jobs, 0, rate_list(args.serve_rates))), flush=True)
+
+
 def run_fock_only(args):
     """Small fixed case for profilers: one job, a few device Fock builds."""
     import torch
@@ -637,6 +650,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision section")
     ap.add_argument("--serve-jobs", type=int, default=12, help="served-stream sample size (0: skip)")
+    ap.add_argument("--serve-rates", default="1,2,4",
+                    help="served stream: arrival rates as multiples of the one-at-a-time FP64 throughput")
+    ap.add_argument("--serve-only", action="store_true", help="run the served-stream section alone")
     ap.add_argument("--scan-points", type=int, default=64,
                     help="batched-scan section: points of each 64-point scan (64: the full 64+64; 0: skip)")
     ap.add_argument("--fock-only", action="store_true",
@@ -649,6 +665,8 @@ def main():
     args = ap.parse_args()
     if args.fock_only:
         run_fock_only(args)
+    elif args.serve_only:
+        run_serve_only(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -120,7 +120,9 @@ __host__ __device__ constexpr int coef_off(int la, int lb, int ab)
     return o;
 }
 __host__ __device__ constexpr int n_coef(int la, int lb) { return coef_off(la, lb, c_nc(la) * c_nc(lb)); }
-__host__ __device__ constexpr int rec_stride(int la, int lb) { return (5 + n_coef(la, lb) + 1) & ~1; }
+// record length: header + coefficients, padded to a multiple of 4 elements
+// (records start 16-byte aligned in FP32 and 32-byte aligned in FP64)
+__host__ __device__ constexpr int rec_stride(int la, int lb) { return (5 + n_coef(la, lb) + 3) & ~3; }
 
 
 // F_0..F_L: table + Taylor for F_L and exp(-T), downward recursion; beyond
@@ -128,48 +130,85 @@ __host__ __device__ constexpr int rec_stride(int la, int lb) { return (5 + n_coe
 template <typename T, int L>
 __device__ __forceinline__ void boys_all(T Tv, const T* __restrict__ tab, T (&F)[L + 1])
 {
-    if (Tv < (T)kBoysTMax) {
-        const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
+    if constexpr (sizeof(T) == 4) {
+        // FP32: both forms, then a select per order (no divergence inside a
+        // warp whose lanes straddle T = 36): the table row of (L, k) as two
+        // 16-byte loads, Taylor + downward recursion; and the asymptotic
+        // F_0 = sqrt(pi/T)/2 with upward recursion (exp(-T) < 3e-16 there)
+        const bool in_table = Tv < (T)kBoysTMax;
+        const int k = in_table ? (int)(Tv * (T)kBoysInvStep + (T)0.5) : 0;
         const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
-        const T* f = tab + k * kBoysM + L;
-        T r;
-        if constexpr (sizeof(T) == 8) {
-            r = __ldg(f + 6) * (T)(1.0 / 720.0);
-            r = fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
-            r = fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
-        } else {
-            r = __ldg(f + 4) * (T)(1.0 / 24.0);
-        }
-        r = fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
-        r = fma(r, nd, __ldg(f + 2) * (T)0.5);
-        r = fma(r, nd, __ldg(f + 1));
-        F[L] = fma(r, nd, __ldg(f));
+        const float4* row = reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysN + k) * kBoys32Row);
+        const float4 c0 = __ldg(row), c1 = __ldg(row + 1);
+        T Ft[L + 1];
+        T r = c1.x;                       // F_{L+4}/24
+        r = fma(r, nd, c0.w);             // F_{L+3}/6
+        r = fma(r, nd, c0.z);             // F_{L+2}/2
+        r = fma(r, nd, c0.y);             // F_{L+1}
+        Ft[L] = fma(r, nd, c0.x);
         if constexpr (L > 0) {
-            T x;
-            if constexpr (sizeof(T) == 8) {
-                x = (T)(1.0 / 5040.0);
-                x = fma(x, nd, (T)(1.0 / 720.0));
-                x = fma(x, nd, (T)(1.0 / 120.0));
-                x = fma(x, nd, (T)(1.0 / 24.0));
-            } else {
-                x = (T)(1.0 / 24.0);
-            }
+            T x = (T)(1.0 / 24.0);
             x = fma(x, nd, (T)(1.0 / 6.0));
             x = fma(x, nd, (T)0.5);
             x = fma(x, nd, (T)1);
             x = fma(x, nd, (T)1);
-            const T e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+            const T e = c1.y * x;
             const T t2 = Tv + Tv;
 #pragma unroll
-            for (int m = L - 1; m >= 0; --m) F[m] = fma(t2, F[m + 1], e) * ((T)1 / (T)(2 * m + 1));
+            for (int m = L - 1; m >= 0; --m) Ft[m] = fma(t2, Ft[m + 1], e) * ((T)1 / (T)(2 * m + 1));
+        }
+        const T rs = rsqrt(fmax(Tv, (T)1e-30));
+        T Fa = (T)0.88622692545275801365 * rs;
+        const T inv2T = (T)0.5 * rs * rs;
+#pragma unroll
+        for (int m = 0; m <= L; ++m) {
+            F[m] = in_table ? Ft[m] : Fa;
+            Fa = (T)(2 * m + 1) * Fa * inv2T;
         }
     } else {
-        const T rs = rsqrt(Tv);
-        F[0] = (T)0.88622692545275801365 * rs;
-        if constexpr (L > 0) {
-            const T inv2T = (T)0.5 * rs * rs;
-#pragma unroll
-            for (int m = 0; m < L; ++m) F[m + 1] = (T)(2 * m + 1) * F[m] * inv2T;
+        if (Tv < (T)kBoysTMax) {
+            const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
+            const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+            const T* f = tab + k * kBoysM + L;
+            T r;
+            if constexpr (sizeof(T) == 8) {
+                r = __ldg(f + 6) * (T)(1.0 / 720.0);
+                r = fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
+                r = fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
+            } else {
+                r = __ldg(f + 4) * (T)(1.0 / 24.0);
+            }
+            r = fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
+            r = fma(r, nd, __ldg(f + 2) * (T)0.5);
+            r = fma(r, nd, __ldg(f + 1));
+            F[L] = fma(r, nd, __ldg(f));
+            if constexpr (L > 0) {
+                T x;
+                if constexpr (sizeof(T) == 8) {
+                    x = (T)(1.0 / 5040.0);
+                    x = fma(x, nd, (T)(1.0 / 720.0));
+                    x = fma(x, nd, (T)(1.0 / 120.0));
+                    x = fma(x, nd, (T)(1.0 / 24.0));
+                } else {
+                    x = (T)(1.0 / 24.0);
+                }
+                x = fma(x, nd, (T)(1.0 / 6.0));
+                x = fma(x, nd, (T)0.5);
+                x = fma(x, nd, (T)1);
+                x = fma(x, nd, (T)1);
+                const T e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+                const T t2 = Tv + Tv;
+    #pragma unroll
+                for (int m = L - 1; m >= 0; --m) F[m] = fma(t2, F[m + 1], e) * ((T)1 / (T)(2 * m + 1));
+            }
+        } else {
+            const T rs = rsqrt(Tv);
+            F[0] = (T)0.88622692545275801365 * rs;
+            if constexpr (L > 0) {
+                const T inv2T = (T)0.5 * rs * rs;
+    #pragma unroll
+                for (int m = 0; m < L; ++m) F[m + 1] = (T)(2 * m + 1) * F[m] * inv2T;
+            }
         }
     }
 }
@@ -205,6 +244,25 @@ __device__ __forceinline__ void hermite_R(T X, T Y, T Z, const T (&s)[L + 1], T 
         });
         R[0] = s[n];
     });
+}
+
+// (p, Px, Py, Pz) of a primitive-pair record: one 16-byte load in FP32
+// (records are 16-byte aligned), four loads in FP64
+template <typename T>
+__device__ __forceinline__ void load_header(const T* r, T& p, T& x, T& y, T& z)
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 h = __ldg(reinterpret_cast<const float4*>(r));
+        p = h.x;
+        x = h.y;
+        y = h.z;
+        z = h.w;
+    } else {
+        p = __ldg(r);
+        x = __ldg(r + 1);
+        y = __ldg(r + 2);
+        z = __ldg(r + 3);
+    }
 }
 
 __device__ __forceinline__ long long spidx(int a, int b)
@@ -243,7 +301,9 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
     const int ij1 = tk.i1, kl0 = tk.k0, kl1 = tk.k1;
     for (int ij = tk.i0; ij < ij1; ++ij) {
         const T* rb = recb + ij * SB;
-        const T p = __ldg(rb), Px = __ldg(rb + 1), Py = __ldg(rb + 2), Pz = __ldg(rb + 3), rp = __ldg(rb + 4);
+        T p, Px, Py, Pz;
+        load_header(rb, p, Px, Py, Pz);
+        const T rp = __ldg(rb + 4);
         const T* cb = rb + 5;
         // kAmortizeBra: the ket-transformed integrals of every ket component
         // pair are summed over the task's ket primitive pairs first
@@ -260,7 +320,9 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
         }
         for (int kl = kl0; kl < kl1; ++kl) {
             const T* rk = reck + kl * SK;
-            const T q = __ldg(rk), Qx = __ldg(rk + 1), Qy = __ldg(rk + 2), Qz = __ldg(rk + 3), rq = __ldg(rk + 4);
+            T q, Qx, Qy, Qz;
+            load_header(rk, q, Qx, Qy, Qz);
+            const T rq = __ldg(rk + 4);
             const T* ck = rk + 5;
             const T X = Px - Qx, Y = Py - Qy, Z = Pz - Qz;
             // 1/sqrt(p+q) is the only root; 1/p, 1/q come with the records
@@ -428,7 +490,7 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
         const int i0 = bra.bf0, j0 = bra.bf1, k0 = ket.bf0, l0 = ket.bf1;
         auto d32 = [&](const T* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
         auto put = [&](double* M, int r, int c, T v) {
-            if (v != (T)0) atomicAdd(M + (long long)r * K + c, (double)v);
+            if (v != (T)0) add_to_fp64<T>(M + (long long)r * K + c, v);
         };
 #pragma unroll
         for (int ab = 0; ab < NAB; ++ab) {

@@ -31,6 +31,12 @@ constexpr int kBoysM = 20;          // orders stored (12 + 7 Taylor terms + 1)
 constexpr int kBoysInvStep = 16;    // grid step 1/16
 constexpr int kBoysTMax = 36;       // table covers [0, 36]; upward recursion beyond
 constexpr int kBoysN = kBoysTMax * kBoysInvStep + 1;
+// FP32 kernels read their own Boys table, one 8-float row per (L, k):
+// {F_L, F_{L+1}, F_{L+2}/2, F_{L+3}/6, F_{L+4}/24, exp(-T_k), 0, 0} at T_k =
+// k/16 (the Taylor terms of F_L about T_k pre-scaled), for L <= kBoys32MaxL,
+// so that one evaluation is two 16-byte loads.
+constexpr int kBoys32MaxL = 12;
+constexpr int kBoys32Row = 8;
 
 // Primitive-pair geometry: p = alpha + beta and the product centre P.
 struct __align__(32) PairGeo {
@@ -213,6 +219,33 @@ struct WarpArgs {
 };
 
 #ifdef __CUDACC__
+// float -> double by bit manipulation on the integer pipes (exact for normal
+// floats; zeros and denormals give a signed zero, infinities and NaNs keep
+// their class).  The FP32 kernels convert their digestion sums this way
+// before the FP64 atomics, since a conversion instruction runs on the FP64
+// pipe, which on this GPU is 1/64 of the FP32 rate.
+__device__ __forceinline__ double f32_to_f64_bits(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned sign = u & 0x80000000u;
+    const unsigned m = u & 0x7fffffu;
+    const unsigned hi_exp = e == 255u ? 0x7ff00000u : ((e + 896u) << 20);
+    const unsigned hi = e == 0u ? sign : (sign | hi_exp | (m >> 3));
+    const unsigned lo = e == 0u ? 0u : (m << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+// Digestion atomics: FP64 accumulators, FP32 sums converted on the integer pipes.
+template <typename T>
+__device__ __forceinline__ void add_to_fp64(double* p, T v)
+{
+    if constexpr (sizeof(T) == 8)
+        atomicAdd(p, v);
+    else
+        atomicAdd(p, f32_to_f64_bits(v));
+}
+
 // Density-weighted Schwarz test of a quartet: the largest density block its
 // J and K contributions touch (AB, CD, AC, AD, BC, BD) times Q_AB Q_CD.
 __device__ __forceinline__ bool density_negligible(const DPair& b, const DPair& k, const double* Dsh, double dthr)

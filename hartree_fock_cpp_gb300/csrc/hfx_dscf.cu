@@ -383,7 +383,7 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
         const bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - E_prev) < opt.energy_threshold);
         E_prev = E_cur;
         out.last_rmsd = rm;
-        if (phase == 0 && to_fp64.update(rm)) phase = 1;
+        if (phase == 0 && to_fp64.update(rm, en)) phase = 1;
         bool done = false;
         if (rm < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
             // final check at the new densities

@@ -201,8 +201,7 @@ void Job::init(const hfx_options& opt)
 
     const std::vector<double>& tab = boys_table_host();
     d_boys_.upload(tab, stream_);
-    std::vector<float> tab32(tab.begin(), tab.end());
-    d_boys32_.upload(tab32, stream_);
+    d_boys32_.upload(boys_table32_host(), stream_);
     for (int s = 0; s < 3; ++s) {
         cudaStream_t st;
         cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -279,6 +278,23 @@ const std::vector<double>& boys_table_host()
     return tab;
 }
 
+const std::vector<float>& boys_table32_host()
+{
+    static const std::vector<float> t32 = [] {
+        const std::vector<double>& t = boys_table_host();
+        std::vector<float> v((size_t)(kBoys32MaxL + 1) * kBoysN * kBoys32Row, 0.0f);
+        const double fac[5] = {1.0, 1.0, 0.5, 1.0 / 6.0, 1.0 / 24.0};
+        for (int L = 0; L <= kBoys32MaxL; ++L)
+            for (int k = 0; k < kBoysN; ++k) {
+                float* r = &v[((size_t)L * kBoysN + k) * kBoys32Row];
+                for (int j = 0; j < 5; ++j) r[j] = (float)(t[(size_t)k * kBoysM + L + j] * fac[j]);
+                r[5] = (float)t[(size_t)k * kBoysM + (kBoysM - 1)];
+            }
+        return v;
+    }();
+    return t32;
+}
+
 // Task order of a launch group: largest cost first, so that the work queues
 // hand out the long tasks early and the threads of a warp get tasks of about
 // the same cost.  Counting sort on 1/16-octave cost bins (stable within a
@@ -346,7 +362,7 @@ const ClassTables& class_tables()
                     }
                 t.ab_start.push_back(k);
                 pt.ncoef = k;
-                pt.stride = (5 + k + 1) & ~1;
+                pt.stride = (5 + k + 3) & ~3;   // rec_stride (hfx_class.cuh): 16-byte aligned records
                 t.tab.push_back(pt);
             }
         return t;

@@ -35,6 +35,8 @@ constexpr int kDefaultLaneMinNpp = 6;
 bool is_small_class(int pcb, int pck, bool fp32);
 // Boys table of the kernels ([kBoysN][kBoysM], last column exp(-T_k)), built once per process.
 const std::vector<double>& boys_table_host();
+// The FP32 kernels' Boys table: 8 floats per (L <= kBoys32MaxL, k), see hfx_device.cuh.
+const std::vector<float>& boys_table32_host();
 
 void cuda_check(cudaError_t e, const char* what);
 

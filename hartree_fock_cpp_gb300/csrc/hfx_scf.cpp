@@ -245,7 +245,7 @@ ScfOutput rhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
         bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - out.E_prev) < opt.energy_threshold);
         out.E_prev = E_cur;
         out.last_rmsd = Pd;
-        if (phase == 0 && to_fp64.update(Pd)) phase = 1;
+        if (phase == 0 && to_fp64.update(Pd, en)) phase = 1;
         if (Pd < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
             // rhf_final_check (scf.hpp:107-137)
             build(Pn, G);
@@ -383,7 +383,7 @@ ScfOutput uhf_diis(const Basis& b, const ScfSetup& setup, const hfx_scf_options&
         bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - out.E_prev) < opt.energy_threshold);
         out.E_prev = E_cur;
         out.last_rmsd = std::max(da, db);
-        if (phase == 0 && to_fp64.update(std::max(da, db))) phase = 1;
+        if (phase == 0 && to_fp64.update(std::max(da, db), en)) phase = 1;
         if (da < opt.epsilon && db < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
             // uhf_final_check (scf.hpp:140-185)
             build(Pan, Pbn);

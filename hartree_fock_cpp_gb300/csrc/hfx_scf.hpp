@@ -19,30 +19,31 @@ using GBuilder = std::function<void(const double* P, double* G, int mode)>;
 // UHF builder: (Pa, Pb) -> J[Pa+Pb], K[Pa], K[Pb].
 using JKBuilder = std::function<void(const double* Pa, const double* Pb, double* J, double* Ka, double* Kb, int mode)>;
 
-// When the mixed-precision SCF leaves its FP32 phase: once RMSD(P) is
-// within a few epsilon of convergence (the last cycles then run as FP64
-// builds -- one full, then FP64 builds of the density change), or earlier
-// if the mixed-precision iterations stop making progress -- no new low of
-// RMSD(P) by at least 10% in four iterations, checked from the eighth
-// iteration on (DIIS is running by then) -- which is where the FP32
-// quartets' error would hold the SCF back.
+// When the mixed-precision SCF leaves its FP32 phase.  The FP32 quartets put
+// a floor under the commutator error ||FPS - SPF|| that the convergence test
+// cannot pass, so the last cycles run in FP64 (one full build, then FP64
+// builds of the density change).  The switch comes once the error norm and
+// RMSD(P) are within 10 epsilon of the target, or when the error norm stops
+// falling -- no new low by at least 10% in four iterations, checked from the
+// eighth iteration on (DIIS is running by then) -- which is where the FP32
+// error floor holds the SCF back.
 class MixedPhaseSwitch {
 public:
     explicit MixedPhaseSwitch(double epsilon) : tol_(kSwitchFactor * epsilon) {}
     // true once the FP32 phase should end; call once per iteration
-    bool update(double rmsd)
+    bool update(double rmsd, double err_norm)
     {
         ++n_;
-        if (rmsd < tol_) return true;
-        if (rmsd < 0.9 * best_) {
-            best_ = rmsd;
+        if (rmsd < tol_ && err_norm < tol_) return true;
+        if (err_norm < 0.9 * best_) {
+            best_ = err_norm;
             since_ = 0;
         } else {
             ++since_;
         }
         return n_ >= kMinIterations && since_ >= kStallIterations;
     }
-    static constexpr double kSwitchFactor = 2.0;
+    static constexpr double kSwitchFactor = 10.0;
     static constexpr int kMinIterations = 8, kStallIterations = 4;
 
 private:

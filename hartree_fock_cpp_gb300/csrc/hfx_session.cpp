@@ -62,8 +62,7 @@ FockSession::FockSession(int device, int nspin, double screening_threshold)
     anchor32_.alloc(64);
     const std::vector<double>& tab = boys_table_host();
     boys64_.upload(tab, stream_);
-    std::vector<float> tab32(tab.begin(), tab.end());
-    boys32_.upload(tab32, stream_);
+    boys32_.upload(boys_table32_host(), stream_);
     const ClassTables& ct = class_tables();
     pct_.upload(ct.tab, stream_);
     abs_.upload(ct.ab_start, stream_);

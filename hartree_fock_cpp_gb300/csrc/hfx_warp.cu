@@ -39,6 +39,32 @@ __device__ __forceinline__ T w_fma(T a, T b, T c)
 template <typename T>
 __device__ __forceinline__ void boys_top(T Tv, int L, const T* __restrict__ tab, T& FL, T& e, bool& table)
 {
+    if constexpr (sizeof(T) == 4) {
+        // FP32 table: one 8-float row per (L, k), Taylor terms pre-scaled
+        if (Tv < (T)kBoysTMax) {
+            table = true;
+            const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
+            const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+            const float4* row = reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysN + k) * kBoys32Row);
+            const float4 c0 = __ldg(row), c1 = __ldg(row + 1);
+            T r = c1.x;
+            r = w_fma(r, nd, c0.w);
+            r = w_fma(r, nd, c0.z);
+            r = w_fma(r, nd, c0.y);
+            FL = w_fma(r, nd, c0.x);
+            T x = (T)(1.0 / 24.0);
+            x = w_fma(x, nd, (T)(1.0 / 6.0));
+            x = w_fma(x, nd, (T)0.5);
+            x = w_fma(x, nd, (T)1);
+            x = w_fma(x, nd, (T)1);
+            e = c1.y * x;
+        } else {
+            table = false;
+            FL = (T)0;
+            e = (T)0;
+        }
+        return;
+    }
     if (Tv < (T)kBoysTMax) {
         table = true;
         int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
@@ -459,7 +485,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
             const T* __restrict__ Dj32 = density_of<T>(a.Dj, a.Dj32) + bra.moff;
             auto d32 = [&](const T* D, int r, int c) { return __ldg(D + (long long)r * K + c); };
             auto put = [&](double* M, int r, int c, T v) {
-                if (v != (T)0) atomicAdd(M + (long long)r * K + c, (double)v);
+                if (v != (T)0) add_to_fp64<T>(M + (long long)r * K + c, v);
             };
             for (int ab = lane; ab < nab; ab += 32) {
                 T sj = 0;
