@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
+#include <cstdio>
+
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -383,6 +385,9 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
         const bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - E_prev) < opt.energy_threshold);
         E_prev = E_cur;
         out.last_rmsd = rm;
+        if (opt.verbose)
+            std::fprintf(stderr, "scf iteration %3d  phase %d  E %.12f  rmsd(P) %.3e  ||FPS-SPF|| %.3e\n", n_it, phase,
+                         E_cur + out.E_nuc, rm, en);
         if (phase == 0 && to_fp64.update(rm, en)) phase = 1;
         bool done = false;
         if (rm < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
