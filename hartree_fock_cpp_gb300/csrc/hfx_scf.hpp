@@ -24,9 +24,10 @@ using JKBuilder = std::function<void(const double* Pa, const double* Pb, double*
 // cannot pass, so the last cycles run in FP64 (one full build, then FP64
 // builds of the density change).  The switch comes once the error norm and
 // RMSD(P) are within 10 epsilon of the target, or when the error norm stops
-// falling -- no new low by at least 10% in four iterations, checked from the
-// eighth iteration on (DIIS is running by then) -- which is where the FP32
-// error floor holds the SCF back.
+// falling -- no new low by at least 10% in four iterations -- after it has
+// come below kStallFloor: that is where the FP32 error floor holds the SCF
+// back.  (Above it, the reference's DIIS can itself pause for a few
+// iterations with an unchanged density, in FP64 as well.)
 class MixedPhaseSwitch {
 public:
     explicit MixedPhaseSwitch(double epsilon) : tol_(kSwitchFactor * epsilon) {}
@@ -41,10 +42,11 @@ public:
         } else {
             ++since_;
         }
-        return n_ >= kMinIterations && since_ >= kStallIterations;
+        return best_ < kStallFloor && since_ >= kStallIterations;
     }
     static constexpr double kSwitchFactor = 10.0;
-    static constexpr int kMinIterations = 8, kStallIterations = 4;
+    static constexpr double kStallFloor = 1e-3;   // ||FPS - SPF|| (Eh)
+    static constexpr int kStallIterations = 4;
 
 private:
     double tol_;
