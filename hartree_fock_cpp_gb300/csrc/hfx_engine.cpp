@@ -300,10 +300,22 @@ const std::vector<float>& boys_table32_host()
 // the same cost.  Counting sort on 1/16-octave cost bins (stable within a
 // bin): O(n), where a comparison sort of a million-task plan took tens of
 // milliseconds of job setup.
-static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost)
+// With `shape` (thread-kernel groups: bra x ket primitive-pair counts of the
+// task, 8 bits each), tasks of one cost bin are further ordered by shape, so
+// that the 32 threads of a warp run loops of the same trip counts.
+static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost,
+                                              const std::vector<unsigned short>* shape = nullptr)
 {
     constexpr int kBins = 1024;
     const size_t n = cost.size();
+    std::vector<size_t> pre;   // stable pre-order by shape
+    if (shape) {
+        std::vector<size_t> cs(65537, 0);
+        for (size_t i = 0; i < n; ++i) ++cs[(*shape)[i] + 1];
+        for (int b = 0; b < 65536; ++b) cs[b + 1] += cs[b];
+        pre.resize(n);
+        for (size_t i = 0; i < n; ++i) pre[cs[(*shape)[i]]++] = i;
+    }
     std::vector<unsigned short> bin(n);
     std::vector<size_t> count(kBins + 1, 0);
     for (size_t i = 0; i < n; ++i) {
@@ -315,7 +327,10 @@ static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost)
     }
     for (int b = 0; b < kBins; ++b) count[b + 1] += count[b];
     std::vector<size_t> idx(n);
-    for (size_t i = 0; i < n; ++i) idx[count[bin[i]]++] = i;
+    for (size_t r = 0; r < n; ++r) {
+        const size_t i = shape ? pre[r] : r;
+        idx[count[bin[i]]++] = i;
+    }
     return idx;
 }
 
@@ -658,6 +673,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         double prims = 0.0;                   // their primitive quartets
         std::vector<Task> t;
         std::vector<double> cost;
+        std::vector<unsigned short> shape;    // (bra, ket) primitive pairs of a task, 8 bits each
     };
     std::vector<Bucket> small(2 * 100), warp(2);
     for_each_surviving_quartet(thr, [&](int X, int Y) {
@@ -706,6 +722,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                     const int k0 = (int)((long long)k.npp * y / nk), k1 = (int)((long long)k.npp * (y + 1) / nk);
                     bk.t.push_back(make_task(bq.first, bq.second, i0, i1, k0, k1));
                     bk.cost.push_back((double)(i1 - i0) * (k1 - k0) * fpp);
+                    if (sm) bk.shape.push_back((unsigned short)(std::min(i1 - i0, 255) * 256 + std::min(k1 - k0, 255)));
                 }
             }
         }
@@ -719,7 +736,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();
     gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
-    auto sorted = [](Bucket& bk) { return order_by_cost_desc(bk.cost); };
+    auto sorted = [](Bucket& bk) { return order_by_cost_desc(bk.cost, bk.shape.empty() ? nullptr : &bk.shape); };
     for (int f = 0; f < 2; ++f)
         for (int pcb = 0; pcb < 10; ++pcb)
             for (int pck = 0; pck <= pcb; ++pck) {
