@@ -35,6 +35,7 @@ public:
     bool update(double rmsd, double err_norm)
     {
         ++n_;
+        if (n_ < kFirstTracked) return false;   // zero-density start, damped iterations
         if (rmsd < tol_ && err_norm < tol_) return true;
         if (err_norm < 0.9 * best_) {
             best_ = err_norm;
@@ -47,6 +48,7 @@ public:
     static constexpr double kSwitchFactor = 10.0;
     static constexpr double kStallFloor = 1e-3;   // ||FPS - SPF|| (Eh)
     static constexpr int kStallIterations = 4;
+    static constexpr int kFirstTracked = 4;        // the first DIIS iteration
 
 private:
     double tol_;
