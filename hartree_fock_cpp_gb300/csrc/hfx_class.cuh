@@ -136,8 +136,8 @@ __device__ __forceinline__ void boys_all(T Tv, const T* __restrict__ tab, T (&F)
         // 16-byte loads, Taylor + downward recursion; and the asymptotic
         // F_0 = sqrt(pi/T)/2 with upward recursion (exp(-T) < 3e-16 there)
         const bool in_table = Tv < (T)kBoysTMax;
-        const int k = in_table ? (int)(Tv * (T)kBoysInvStep + (T)0.5) : 0;
-        const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+        int k;
+        const T nd = boys_grid_offset(in_table ? Tv : (T)0, k);
         const float4* row = reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysN + k) * kBoys32Row);
         const float4 c0 = __ldg(row), c1 = __ldg(row + 1);
         T Ft[L + 1];
@@ -482,7 +482,7 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
                 const long long pkl = spidx(k, l);
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) || (same_pair && pij < pkl) ||
                                   (screen && qb * __ldg(QbT + pkl) < thrT);
-                const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
+                const T f = (i == j ? (T)1 : (T)2) * (k == l ? (T)1 : (T)2) * (pij == pkl ? (T)1 : (T)2);
                 acc[ab][cd] = skip ? (T)0 : acc[ab][cd] * f;
             }
         }

@@ -236,6 +236,17 @@ __device__ __forceinline__ double f32_to_f64_bits(float v)
     return __hiloint2double((int)hi, (int)lo);
 }
 
+// Nearest Boys-table grid point of T (0 <= T < 2^18): k = round(16 T) and the
+// Taylor step nd = k/16 - T, without conversion instructions (adding 1.5 * 2^23
+// leaves round(16 T) in the float's low mantissa bits).
+__device__ __forceinline__ float boys_grid_offset(float T, int& k)
+{
+    const float magic = 12582912.0f;
+    const float t = fmaf(T, (float)kBoysInvStep, magic);
+    k = __float_as_int(t) - __float_as_int(magic);
+    return (t - magic) * (1.0f / (float)kBoysInvStep) - T;
+}
+
 // Digestion atomics: FP64 accumulators, FP32 sums converted on the integer pipes.
 template <typename T>
 __device__ __forceinline__ void add_to_fp64(double* p, T v)

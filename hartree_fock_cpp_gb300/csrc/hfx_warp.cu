@@ -43,8 +43,8 @@ __device__ __forceinline__ void boys_top(T Tv, int L, const T* __restrict__ tab,
         // FP32 table: one 8-float row per (L, k), Taylor terms pre-scaled
         if (Tv < (T)kBoysTMax) {
             table = true;
-            const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
-            const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
+            int k;
+            const T nd = boys_grid_offset(Tv, k);
             const float4* row = reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysN + k) * kBoys32Row);
             const float4 c0 = __ldg(row), c1 = __ldg(row + 1);
             T r = c1.x;
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(256) k_warp_quartet(WarpArgs<T> a)
                 const bool skip = (bra.same && ia < ib) || (ket.same && ic < id) ||
                                   (task.bra == task.ket && pij < pkl) ||
                                   (screen && __ldg(QbT + pij) * __ldg(QbT + pkl) < thrT);
-                const T f = (T)((i == j ? 1 : 2) * (k == l ? 1 : 2) * (pij == pkl ? 1 : 2));
+                const T f = (i == j ? (T)1 : (T)2) * (k == l ? (T)1 : (T)2) * (pij == pkl ? (T)1 : (T)2);
                 acc[e] = skip ? (T)0 : acc[e] * f;
             }
             __syncwarp();
