@@ -155,3 +155,25 @@ def test_packed_admission_within_a_small_memory_budget():
     for inf in infos:
         assert inf["state"] == "done" and inf["converged"], inf
     assert st["in_use_bytes"] == 0
+
+
+@pytest.mark.parametrize("pack_max", [0, 8])
+def test_mixed_precision_requests_same_alone_and_served(pack_max):
+    """Mixed-precision requests (RHF and UHF) follow the mixed-precision SCF
+    protocol in the server as they do alone (FP32 builds, then FP64 final
+    cycles): the same energies and iteration counts, per-job and packed."""
+    jobs = [dict(config=W.water(), basis_set="cc-pVDZ", method="RHF"),
+            dict(config=OH, basis_set="6-31G*", method="UHF", spin=(5, 4)),
+            dict(config=W.benzene(), basis_set="cc-pVDZ", method="RHF")]
+    kw = dict(precision=H.HFX_PREC_MIXED, fp32_threshold=0.03)
+    alone = [H.uhf_diis(j["config"], j["basis_set"], spin_occ=j["spin"], **kw) if j["method"] == "UHF"
+             else H.rhf_diis(j["config"], j["basis_set"], **kw) for j in jobs]
+    assert sum(a["mixed_builds"] for a in alone) > 0
+    with Server(max_active=4, pack_max=pack_max, precision=H.HFX_PREC_MIXED, fp32_threshold=0.03) as srv:
+        ids = [srv.submit(**j) for j in jobs]
+        srv.drain(600)
+        infos = [srv.poll(i) for i in ids]
+    for a, inf in zip(alone, infos):
+        assert inf["state"] == "done" and inf["converged"], inf
+        assert abs(inf["E_tot"] - a["E_tot"]) < E_TOL
+        assert abs(inf["iterations"] - a["iterations"]) <= 1
