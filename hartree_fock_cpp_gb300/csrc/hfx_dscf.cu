@@ -20,6 +20,8 @@
 #include <cusolverDn.h>
 
 #include <cstdio>
+#include <mutex>
+#include <map>
 
 #include <chrono>
 #include <cmath>
@@ -73,12 +75,56 @@ __global__ void k_lincomb(int n, Coef8 cf, double* C)
 
 static int grid_for(int n) { return std::min(1024, std::max(1, (n + 255) / 256)); }
 
+// cuBLAS / cuSOLVER handles, kept per device for reuse: creating them costs
+// tens of milliseconds, which every SCF of the request server and of a
+// scan's chained points would otherwise pay.  A handle pair serves one
+// DeviceScf at a time.
+namespace {
+struct HandlePair {
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+};
+std::mutex g_handle_mu;
+std::map<int, std::vector<HandlePair>> g_handles;
+
+HandlePair acquire_handles()
+{
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    {
+        std::lock_guard<std::mutex> lk(g_handle_mu);
+        auto& v = g_handles[dev];
+        if (!v.empty()) {
+            HandlePair h = v.back();
+            v.pop_back();
+            return h;
+        }
+    }
+    HandlePair h;
+    cublas_check(cublasCreate(&h.blas), "create");
+    if (cusolverDnCreate(&h.solver) != CUSOLVER_STATUS_SUCCESS) {
+        cublasDestroy(h.blas);
+        throw Error(HFX_ERR_CUDA, "cusolverDnCreate failed");
+    }
+    return h;
+}
+
+void release_handles(HandlePair h)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lk(g_handle_mu);
+    g_handles[dev].push_back(h);
+}
+}  // namespace
+
 DeviceScf::DeviceScf(FockSource& job, const ScfSetup& setup, int nspin) : job_(job), K_(job.K()), nspin_(nspin)
 {
     st_ = job.stream();
-    cublas_check(cublasCreate(&blas_), "create");
+    HandlePair h = acquire_handles();
+    blas_ = h.blas;
+    solver_ = h.solver;
     cublas_check(cublasSetStream(blas_, st_), "stream");
-    cusolver_check(cusolverDnCreate(&solver_), "create");
     cusolver_check(cusolverDnSetStream(solver_, st_), "stream");
     const size_t n = (size_t)K_ * K_;
     H_.upload(setup.H, st_);
@@ -117,8 +163,8 @@ DeviceScf::DeviceScf(FockSource& job, const ScfSetup& setup, int nspin) : job_(j
 
 DeviceScf::~DeviceScf()
 {
-    if (solver_) cusolverDnDestroy(solver_);
-    if (blas_) cublasDestroy(blas_);
+    if (st_) cudaStreamSynchronize(st_);
+    if (blas_ && solver_) release_handles(HandlePair{blas_, solver_});
 }
 
 void DeviceScf::gemm(bool ta, const double* A, bool tb, const double* B, double* C, double alpha, int kdim)
