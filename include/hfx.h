@@ -210,10 +210,9 @@ typedef struct {
     int charge;
     int precision;              /* HFX_PREC_FP64 / HFX_PREC_MIXED */
     double fp32_threshold;      /* mixed precision cut (see hfx_options) */
-    int fp64_final_cycles;      /* mixed: once RMSD(P) and ||FPS-SPF|| < 10 eps, or when ||FPS-SPF|| (below 1e-3)
-                                   stops falling (no new low by 10% in four iterations), switch to one full FP64
-                                   build and FP64 builds of the density change (default 0 = on; -1: full FP64
-                                   builds instead) */
+    int fp64_final_cycles;      /* mixed: once ||FPS-SPF|| < 1000 eps, or when it (below 1e-3) stops falling (no new
+                                   low by 10% in four iterations), switch to one full FP64 build and FP64 builds
+                                   of the density change (default 0 = on; -1: full FP64 builds instead) */
     int start_diis;             /* default 4 (scf.hpp:235) */
     int max_history;            /* default 8 (scf.hpp:236) */
     int verbose;
