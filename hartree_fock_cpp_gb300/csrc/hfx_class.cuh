@@ -318,6 +318,9 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
 #pragma unroll
                 for (int h = 0; h < H1; ++h) Wt[cd][h] = (T)0;
         }
+        // the low-L classes are bound by the latency of the record and Boys-table
+        // loads: two ket primitive pairs in flight per thread
+#pragma unroll(L <= 2 ? 2 : 1)
         for (int kl = kl0; kl < kl1; ++kl) {
             const T* rk = reck + kl * SK;
             T q, Qx, Qy, Qz;
