@@ -385,6 +385,10 @@ const ClassTables& class_tables()
     return ct;
 }
 
+// Primitive pairs below this fraction of their shell pair's largest
+// coefficient are left out (build_pair_data).
+constexpr double kPrimPairCut = 1e-14;
+
 PairData build_pair_data(const Basis& basis, const Fragments& fr)
 {
     const ClassTables& ct = class_tables();
@@ -412,26 +416,34 @@ PairData build_pair_data(const Basis& basis, const Fragments& fr)
             const int pc = pair_class(l0, l1);
             const PairClassTab& pt = ct.tab[pc];
             const long long rec_off = (long long)pd.rec.size();
-            int npp = 0;
             int nt = L + 1;
+            // All primitive pairs of the shell pair first (geometry, dense E
+            // block, record coefficients), then only those whose largest
+            // Hermite->Cartesian coefficient reaches kPrimPairCut of the shell
+            // pair's largest: the others (tight primitives on distant centres,
+            // exp(-mu |AB|^2) ~ 0) change no integral by more than ~1e-14 of
+            // its size, and skipping them removes their primitive quartets
+            // from every class kernel.
+            struct Prim {
+                double p, x, y, z, cmax;
+                std::vector<double> e, c;
+            };
+            std::vector<Prim> prims;
+            double cmax_pair = 0.0;
             for (int i = 0; i < S0.nprim(); ++i)
                 for (int j = 0; j < S1.nprim(); ++j) {
                     double a = S0.exps[i], be = S1.exps[j], p = a + be;
                     hermite_1d(l0, l1, a, be, S0.x, S1.x, Ex);
                     hermite_1d(l0, l1, a, be, S0.y, S1.y, Ey);
                     hermite_1d(l0, l1, a, be, S0.z, S1.z, Ez);
-                    pd.geo.push_back(make_pairgeo(p, (a * S0.x + be * S1.x) / p, (a * S0.y + be * S1.y) / p,
-                                                  (a * S0.z + be * S1.z) / p));
-                    size_t base = pd.epool.size();
-                    pd.epool.resize(base + (size_t)n0 * n1 * H, 0.0);
-                    size_t rb = pd.rec.size();
-                    pd.rec.resize(rb + pt.stride, 0.0);
-                    pd.rec[rb] = p;
-                    pd.rec[rb + 1] = (a * S0.x + be * S1.x) / p;
-                    pd.rec[rb + 2] = (a * S0.y + be * S1.y) / p;
-                    pd.rec[rb + 3] = (a * S0.z + be * S1.z) / p;
-                    pd.rec[rb + 4] = 1.0 / p;
-                    int kc = 0;
+                    Prim pr;
+                    pr.p = p;
+                    pr.x = (a * S0.x + be * S1.x) / p;
+                    pr.y = (a * S0.y + be * S1.y) / p;
+                    pr.z = (a * S0.z + be * S1.z) / p;
+                    pr.cmax = 0.0;
+                    pr.e.assign((size_t)n0 * n1 * H, 0.0);
+                    pr.c.reserve((size_t)pt.ncoef);
                     for (int c0 = 0; c0 < n0; ++c0) {
                         int ax, ay, az;
                         component(l0, c0, ax, ay, az);
@@ -439,7 +451,7 @@ PairData build_pair_data(const Basis& basis, const Fragments& fr)
                             int bx, by, bz;
                             component(l1, c1, bx, by, bz);
                             double w = S0.w[(size_t)c0 * S0.nprim() + i] * S1.w[(size_t)c1 * S1.nprim() + j];
-                            double* row = pd.epool.data() + base + (size_t)(c0 * n1 + c1) * H;
+                            double* row = pr.e.data() + (size_t)(c0 * n1 + c1) * H;
                             for (int t = 0; t <= ax + bx; ++t)
                                 for (int u = 0; u <= ay + by; ++u)
                                     for (int v = 0; v <= az + bz; ++v) {
@@ -447,12 +459,29 @@ PairData build_pair_data(const Basis& basis, const Fragments& fr)
                                                    Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
                                                    Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
                                         row[herm_index(t, u, v)] = c;
-                                        pd.rec[rb + 5 + kc++] = c;
+                                        pr.c.push_back(c);
+                                        pr.cmax = std::max(pr.cmax, std::fabs(c));
                                     }
                         }
                     }
-                    ++npp;
+                    cmax_pair = std::max(cmax_pair, pr.cmax);
+                    prims.push_back(std::move(pr));
                 }
+            int npp = 0;
+            for (const Prim& pr : prims) {
+                if (pr.cmax < kPrimPairCut * cmax_pair) continue;
+                pd.geo.push_back(make_pairgeo(pr.p, pr.x, pr.y, pr.z));
+                pd.epool.insert(pd.epool.end(), pr.e.begin(), pr.e.end());
+                size_t rb = pd.rec.size();
+                pd.rec.resize(rb + pt.stride, 0.0);
+                pd.rec[rb] = pr.p;
+                pd.rec[rb + 1] = pr.x;
+                pd.rec[rb + 2] = pr.y;
+                pd.rec[rb + 3] = pr.z;
+                pd.rec[rb + 4] = 1.0 / pr.p;
+                for (size_t k = 0; k < pr.c.size(); ++k) pd.rec[rb + 5 + k] = pr.c[k];
+                ++npp;
+            }
             hp.npp = npp;
             DPair d{};
             d.bf0 = S0.bf0 - fr.bf[f];
