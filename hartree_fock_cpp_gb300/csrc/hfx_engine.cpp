@@ -387,7 +387,7 @@ const ClassTables& class_tables()
 
 // Primitive pairs below this fraction of their shell pair's largest
 // coefficient are left out (build_pair_data).
-constexpr double kPrimPairCut = 1e-14;
+constexpr double kPrimPairCut = 1e-18;
 
 PairData build_pair_data(const Basis& basis, const Fragments& fr)
 {
