@@ -364,7 +364,8 @@ def run_engine(args):
         "batched_scans": scans,
         "mixed_precision": mixed,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-        "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val, "reference_iterations": ref_iters},
+        "scf": {"iterations": iters, "fock_builds": builds, "E_tot": E_val, "reference_iterations": ref_iters,
+                "density_step": {"sp2_projections": res.projections, "syevd_fallbacks": res.projection_fallbacks}},
         "fock_builds_per_s": {"fp64": 1e3 / build_ms},
         "eri_rate": {"shell_quartets_per_s": s["quartets"] / (kernel_ms * 1e-3),
                      "primitive_quartets_per_s": s["prim_quartets"] / (kernel_ms * 1e-3),

@@ -22,10 +22,11 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import BASIS_PATH, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError, check, lib, ptr
+from ._lib import BASIS_PATH, HFX_EIG_AUTO, HFX_EIG_SYEVD, HFX_PREC_FP64, HFX_PREC_MIXED, HfxError, check, lib, ptr
 
 __all__ = ["Basis", "basis_construction", "schwarz_bounds", "ERI_GPU", "FockBuilder", "rhf_diis", "uhf_diis",
-           "one_electron", "measure_peaks", "measure_dmma_peak", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED", "BASIS_PATH",
+           "one_electron", "measure_peaks", "measure_dmma_peak", "HfxError", "HFX_PREC_FP64", "HFX_PREC_MIXED",
+           "HFX_EIG_AUTO", "HFX_EIG_SYEVD", "BASIS_PATH",
            "eri_index", "pair_index", "batch_scf"]
 
 
@@ -221,8 +222,9 @@ def ERI_GPU(basis, threshold=1e-8):
 
 
 def _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
-                 fp32_threshold):
+                 fp32_threshold, eigensolver=0):
     o = _lib.ScfOptions()
+    o.eigensolver = eigensolver
     o.max_iterations = max_it
     o.epsilon = epsilon
     o.damping = damping
@@ -243,13 +245,17 @@ def _check_device(eri_device):
 
 def rhf_diis(config, basis_set, param_path=None, charge=0, eri_device="GPU", set_initial_density=False, P0=None,
              max_it=10000, epsilon=1e-6, damping=0.3, screening_threshold=1e-8, energy_threshold=0.0,
-             precision=HFX_PREC_FP64, fp32_threshold=0.0, raise_on_nonconvergence=False):
+             precision=HFX_PREC_FP64, fp32_threshold=0.0, raise_on_nonconvergence=False, eigensolver=HFX_EIG_AUTO,
+             verbose=False):
     """scf.hpp:205-419 with the direct GPU Fock build.  Returns a dict shaped
-    like the reference's rhf_data (types.hpp:50-73)."""
+    like the reference's rhf_data (types.hpp:50-73).  eigensolver: the density
+    step, HFX_EIG_AUTO (SP2 projector, syevd fallback) or HFX_EIG_SYEVD;
+    verbose: one line per iteration on stderr."""
     _check_device(eri_device)
     m = _lib.MoleculeArgs(config, basis_set, param_path)
     o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
-                     fp32_threshold)
+                     fp32_threshold, eigensolver)
+    o.verbose = int(bool(verbose))
     K = ctypes.c_int()
     check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
     K = K.value
@@ -266,18 +272,19 @@ def rhf_diis(config, basis_set, param_path=None, charge=0, eri_device="GPU", set
     return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
                 K=r.K, Ne=r.n_electrons, density=dens, coefficient=coef, mo_energy=mo, duration=r.seconds,
                 fock_ms=r.fock_ms, fock_builds=r.fock_builds, mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds,
-                delta_builds=r.delta_builds, hardware=eri_device, BasisSet=basis_set, charge=charge)
+                delta_builds=r.delta_builds, projections=r.projections,
+                projection_fallbacks=r.projection_fallbacks, hardware=eri_device, BasisSet=basis_set, charge=charge)
 
 
 def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_device="GPU",
              set_initial_density=False, Pa0=None, Pb0=None, max_it=10000, epsilon=1e-6, damping=0.3,
              screening_threshold=1e-8, energy_threshold=0.0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
-             raise_on_nonconvergence=False):
+             raise_on_nonconvergence=False, eigensolver=HFX_EIG_AUTO):
     """scf.hpp:423-682 with the direct GPU J/Ka/Kb build."""
     _check_device(eri_device)
     m = _lib.MoleculeArgs(config, basis_set, param_path)
     o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
-                     fp32_threshold)
+                     fp32_threshold, eigensolver)
     K = ctypes.c_int()
     check(lib.hfx_one_electron(m.ref(), None, None, None, ctypes.byref(K)))
     K = K.value
@@ -296,13 +303,14 @@ def uhf_diis(config, basis_set, param_path=None, spin_occ=(1, 0), charge=0, eri_
     return dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
                 K=r.K, Pa=Pa, Pb=Pb, Ea=ea, Eb=eb, duration=r.seconds, fock_ms=r.fock_ms,
                 fock_builds=r.fock_builds, mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds,
-                delta_builds=r.delta_builds, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
+                delta_builds=r.delta_builds, projections=r.projections,
+                projection_fallbacks=r.projection_fallbacks, Na=int(spin_occ[0]), Nb=int(spin_occ[1]), hardware=eri_device,
                 BasisSet=basis_set, charge=charge)
 
 
 def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsilon=1e-6, damping=0.3,
               screening_threshold=1e-8, energy_threshold=0.0, precision=HFX_PREC_FP64, fp32_threshold=0.0,
-              max_parallel=0, param_path=None, warm_chain=0):
+              max_parallel=0, param_path=None, warm_chain=0, eigensolver=HFX_EIG_AUTO):
     """Lockstep batched SCF (hfx_batch_scf): `molecules` is a list of
     (config, basis_set); all of them iterate together on one packed job, one
     Fock build per SCF cycle over every molecule still iterating.  The
@@ -327,7 +335,7 @@ def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsil
         na = np.ascontiguousarray([int(s[0]) for s in spins], dtype=np.int32)
         nb = np.ascontiguousarray([int(s[1]) for s in spins], dtype=np.int32)
     o = _scf_options(charge, max_it, epsilon, damping, screening_threshold, energy_threshold, precision,
-                     fp32_threshold)
+                     fp32_threshold, eigensolver)
     bo = _lib.BatchOptions()
     bo.method = 1 if uhf else 0
     bo.max_parallel = int(max_parallel)
@@ -340,7 +348,8 @@ def batch_scf(molecules, method="RHF", spins=None, charge=0, max_it=10000, epsil
         check(status)
     out = [dict(E_tot=r.E_tot, E_ele=r.E_ele, E_nuc=r.E_nuc, iterations=r.iterations, converged=bool(r.converged),
                 K=r.K, duration=r.seconds, fock_ms=r.fock_ms, fock_builds=r.fock_builds,
-                mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds, delta_builds=r.delta_builds)
+                mixed_builds=r.mixed_builds, fp64_builds=r.fp64_builds, delta_builds=r.delta_builds, projections=r.projections,
+                projection_fallbacks=r.projection_fallbacks)
            for r in res]
     stats = dict(seconds=st.seconds, setup_seconds=st.setup_seconds, cycles=st.cycles, molecules=st.molecules,
                  build_ms=st.build_ms, quartets=st.quartets, flops_fp64=st.flops_fp64)

@@ -18,6 +18,8 @@ STATUS_NAMES = {0: "HFX_OK", 1: "HFX_ERR_INVALID", 2: "HFX_ERR_BASIS", 3: "HFX_E
                 9: "HFX_ERR_NUMERIC"}
 HFX_PREC_FP64 = 0
 HFX_PREC_MIXED = 1
+HFX_EIG_AUTO = 0
+HFX_EIG_SYEVD = 1
 
 
 class HfxError(RuntimeError):
@@ -58,7 +60,7 @@ class ScfOptions(ctypes.Structure):
                 ("screening_threshold", ctypes.c_double), ("energy_threshold", ctypes.c_double),
                 ("charge", ctypes.c_int), ("precision", ctypes.c_int), ("fp32_threshold", ctypes.c_double),
                 ("fp64_final_cycles", ctypes.c_int), ("start_diis", ctypes.c_int), ("max_history", ctypes.c_int),
-                ("verbose", ctypes.c_int), ("reserved", ctypes.c_int * 6)]
+                ("verbose", ctypes.c_int), ("eigensolver", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class ScfResult(ctypes.Structure):
@@ -66,7 +68,8 @@ class ScfResult(ctypes.Structure):
                 ("iterations", ctypes.c_int), ("converged", ctypes.c_int), ("K", ctypes.c_int),
                 ("n_electrons", ctypes.c_int), ("seconds", ctypes.c_double), ("fock_ms", ctypes.c_double),
                 ("fock_builds", ctypes.c_int), ("mixed_builds", ctypes.c_int), ("fp64_builds", ctypes.c_int),
-                ("delta_builds", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("delta_builds", ctypes.c_int), ("projections", ctypes.c_int),
+                ("projection_fallbacks", ctypes.c_int), ("reserved", ctypes.c_int * 2)]
 
 
 class ServerOptions(ctypes.Structure):

@@ -338,6 +338,8 @@ static void fill_result(const ScfOutput& o, hfx_scf_result* r, double fock_ms)
     r->mixed_builds = o.mixed_builds;
     r->fp64_builds = o.fp64_builds;
     r->delta_builds = o.delta_builds;
+    r->projections = o.projections;
+    r->projection_fallbacks = o.projection_fallbacks;
 }
 
 static hfx_options job_options(const hfx_scf_options* o)

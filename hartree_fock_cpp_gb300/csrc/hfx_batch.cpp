@@ -221,6 +221,8 @@ void fill(const ScfOutput& o, hfx_scf_result* r)
     r->mixed_builds = o.mixed_builds;
     r->fp64_builds = o.fp64_builds;
     r->delta_builds = o.delta_builds;
+    r->projections = o.projections;
+    r->projection_fallbacks = o.projection_fallbacks;
 }
 
 double now_s()

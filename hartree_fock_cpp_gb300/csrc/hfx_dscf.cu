@@ -6,9 +6,13 @@
 // (F, FPS-SPF) pairs with the augmented B matrix solved by complete-pivoting
 // LU, symmetric orthogonalisation, convergence on RMSD(P) and ||FPS-SPF||
 // followed by the final check.  The O(K^3) algebra runs on the job's stream:
-// FP64 GEMMs (cuBLAS), the symmetric eigensolver (cuSOLVER syevd), and small
-// element-wise kernels; only the DIIS system ((n+1) x (n+1), n <= 8) and a
-// handful of scalars per iteration travel to the host.
+// FP64 GEMMs (cuBLAS), the density step (the SP2 projector of hfx_sp2.cu, or
+// the symmetric eigensolver cuSOLVER syevd), and small element-wise kernels;
+// only the DIIS system ((n+1) x (n+1), n <= 8) and a handful of scalars per
+// iteration travel to the host.  The reference diagonalises the Fock matrix
+// every iteration; only the density enters the next iteration, and the
+// projector gives the same density to rounding.  The MO energies and
+// coefficients of the last iteration come from one syevd after the loop.
 //
 // Layout: every matrix is K x K.  The symmetric ones (S, X, H, F, P, G) are
 // the same in row- and column-major order; the others (C, FPS-SPF) are kept
@@ -146,6 +150,7 @@ DeviceScf::DeviceScf(FockSource& job, const ScfSetup& setup, int nspin) : job_(j
         Pr_[s].alloc(n);
         dP_[s].alloc(n);
         e_[s].alloc(K_);
+        Fq_[s].alloc(n);
     }
     G_.alloc(n);
     Kx_[0].alloc(n);
@@ -264,23 +269,51 @@ void DeviceScf::error_and_energy()
     }
 }
 
-// eigenvectors of the (DIIS) Fock matrices -> new densities Pn_, MO
-// energies e_; C_ column-major
-void DeviceScf::diagonalise(const double* const* Fs, const int* nocc, double occ_factor)
+// New densities Pn_ of the (DIIS) Fock matrices: P = f X D X^T with D the
+// projector onto the nocc lowest eigenvectors of F' = X^T F X.  D comes from
+// the SP2 projector (no host synchronisation) when use_proj, else from
+// cuSOLVER syevd, which also gives the MO energies e_ and coefficients C_
+// (column-major); F' stays in Fq_[s] for a later syevd.
+void DeviceScf::diagonalise(const double* const* Fs, const int* nocc, double occ_factor, bool use_proj)
 {
     for (int s = 0; s < nspin_; ++s) {
         gemm(false, Fs[s], false, X_.p, T1_.p);        // F X
-        gemm(true, X_.p, false, T1_.p, Fp_.p);         // X^T F X
-        cusolver_check(cusolverDnDsyevd(solver_, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, K_, Fp_.p, K_,
-                                        e_[s].p, work_.p, lwork_, info_.p),
-                       "syevd");
-        gemm(false, X_.p, false, Fp_.p, C_[s].p);      // C = X C'
-        // P = f C_occ C_occ^T
-        if (nocc[s] > 0) {
-            gemm(false, C_[s].p, true, C_[s].p, Pn_[s].p, occ_factor, nocc[s]);
+        gemm(true, X_.p, false, T1_.p, Fq_[s].p);      // X^T F X
+        proj_[s] = use_proj && nocc[s] > 0 && nocc[s] < K_;
+        if (proj_[s]) {
+            // the step count changes little between SCF iterations
+            project(s, nocc[s], occ_factor, proj_steps_[s] > 0 ? proj_steps_[s] + 5 : Sp2Projector::kMaxSteps);
         } else {
-            cuda_check(cudaMemsetAsync(Pn_[s].p, 0, sizeof(double) * K_ * K_, st_), "memset");
+            eigensolve(s, nocc[s], occ_factor, true);
         }
+    }
+}
+
+void DeviceScf::project(int s, int nocc, double occ_factor, int max_steps)
+{
+    if (!sp2_) {
+        sp2_.reset(new Sp2Projector(K_));
+        D_.alloc((size_t)K_ * K_);
+    }
+    proj_cap_[s] = max_steps;
+    sp2_->run(Fq_[s].p, nocc, D_.p, scal_.p + 2 + s, st_, max_steps);
+    gemm(false, X_.p, false, D_.p, T1_.p);                  // X D
+    gemm(false, T1_.p, true, T1_.p, Pn_[s].p, occ_factor);  // f (X D)(X D)^T = f X D X^T
+}
+
+void DeviceScf::eigensolve(int s, int nocc, double occ_factor, bool density)
+{
+    cuda_check(cudaMemcpyAsync(Fp_.p, Fq_[s].p, sizeof(double) * K_ * K_, cudaMemcpyDeviceToDevice, st_), "copy");
+    cusolver_check(cusolverDnDsyevd(solver_, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, K_, Fp_.p, K_,
+                                    e_[s].p, work_.p, lwork_, info_.p),
+                   "syevd");
+    gemm(false, X_.p, false, Fp_.p, C_[s].p);      // C = X C'
+    if (!density) return;
+    // P = f C_occ C_occ^T
+    if (nocc > 0) {
+        gemm(false, C_[s].p, true, C_[s].p, Pn_[s].p, occ_factor, nocc);
+    } else {
+        cuda_check(cudaMemsetAsync(Pn_[s].p, 0, sizeof(double) * K_ * K_, st_), "memset");
     }
 }
 
@@ -332,6 +365,9 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
     int phase = mixed ? 0 : 2;
     bool have_ref = false;
     MixedPhaseSwitch to_fp64(opt.epsilon);
+    const bool use_proj = opt.eigensolver == HFX_EIG_AUTO && K <= Sp2Projector::kScfMaxN;
+    proj_[0] = proj_[1] = false;
+    proj_steps_[0] = proj_steps_[1] = 0;
     auto do_build = [&]() {
         ++out.fock_builds;
         if (!mixed) {
@@ -419,21 +455,54 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
                 Fuse[s] = E_[s].p;
             }
         }
-        diagonalise(Fuse, nocc, occf);
+        diagonalise(Fuse, nocc, occf, use_proj);
         // RMSD(P_new - P) per spin
         for (int s = 0; s < nspin_; ++s) {
             axpby(1.0, Pn_[s].p, -1.0, P_[s].p, T1_.p);
             dot(T1_.p, T1_.p, n, s);
         }
-        fetch(sc, 2);
+        fetch(sc, 4);
+        // a projection that did not converge within the step cap is repeated
+        // with the full cap; one that did not converge at all (no gap at the
+        // Fermi level) is replaced by an eigensolve
+        double status[2] = {-1.0, -1.0};
+        bool counted[2] = {false, false};
+        for (;;) {
+            bool refetch = false;
+            for (int s = 0; s < nspin_; ++s) {
+                if (!proj_[s] || counted[s]) continue;
+                status[s] = sc[2 + s];
+                if (sc[2 + s] > 0.0) {
+                    ++out.projections;
+                    proj_steps_[s] = (int)sc[2 + s];
+                    counted[s] = true;
+                    continue;
+                }
+                if (proj_cap_[s] < Sp2Projector::kMaxSteps) {
+                    project(s, nocc[s], occf, Sp2Projector::kMaxSteps);
+                } else {
+                    ++out.projection_fallbacks;
+                    proj_[s] = false;
+                    proj_steps_[s] = 0;
+                    eigensolve(s, nocc[s], occf, true);
+                }
+                axpby(1.0, Pn_[s].p, -1.0, P_[s].p, T1_.p);
+                dot(T1_.p, T1_.p, n, s);
+                refetch = true;
+            }
+            if (!refetch) break;
+            fetch(sc, 4);
+        }
         double rm = 0.0;
         for (int s = 0; s < nspin_; ++s) rm = std::max(rm, std::sqrt(sc[s] / n));
         const bool dE_ok = opt.energy_threshold <= 0 || (n_it > 1 && std::fabs(E_cur - E_prev) < opt.energy_threshold);
         E_prev = E_cur;
         out.last_rmsd = rm;
         if (opt.verbose)
-            std::fprintf(stderr, "scf iteration %3d  phase %d  E %.12f  rmsd(P) %.3e  ||FPS-SPF|| %.3e\n", n_it, phase,
-                         E_cur + out.E_nuc, rm, en);
+            std::fprintf(stderr,
+                         "scf iteration %3d  phase %d  E %.12f  rmsd(P) %.3e  ||FPS-SPF|| %.3e  projector steps %d %d "
+                         "(status %g %g)\n",
+                         n_it, phase, E_cur + out.E_nuc, rm, en, proj_steps_[0], proj_steps_[1], status[0], status[1]);
         if (phase == 0 && to_fp64.update(rm, en)) phase = 1;
         bool done = false;
         if (rm < opt.epsilon && en < opt.epsilon && dE_ok && phase != 0) {
@@ -469,6 +538,9 @@ ScfOutput DeviceScf::run(const Basis& b, const ScfSetup& setup, const hfx_scf_op
         }
     }
     out.iterations = n_it;
+    // MO energies and coefficients of the last density step where it was a projection
+    for (int s = 0; s < nspin_; ++s)
+        if (proj_[s]) eigensolve(s, nocc[s], occf, false);
     // results to the host: densities, MO energies, coefficients (row-major)
     out.P.resize(n);
     cuda_check(cudaMemcpyAsync(out.P.data(), P_[0].p, bytes, cudaMemcpyDeviceToHost, st_), "D2H P");

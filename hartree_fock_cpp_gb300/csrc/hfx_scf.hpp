@@ -66,6 +66,7 @@ struct ScfOutput {
     int K = 0, n_electrons = 0;
     int fock_builds = 0;
     int mixed_builds = 0, fp64_builds = 0, delta_builds = 0;
+    int projections = 0, projection_fallbacks = 0;
     double seconds = 0;
     double fock_ms = 0;
     std::vector<double> P, P2, C, e, e2;

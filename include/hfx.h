@@ -54,6 +54,12 @@ enum {
     HFX_PREC_MIXED = 1        /* quartets with Schwarz bound < fp32_threshold in FP32 */
 };
 
+/* Density step of the device SCF (hfx_scf_options.eigensolver). */
+enum {
+    HFX_EIG_AUTO = 0,         /* SP2 projector on the device, syevd fallback */
+    HFX_EIG_SYEVD = 1         /* cuSOLVER syevd every iteration */
+};
+
 /* ---- basis descriptions -------------------------------------------------- */
 
 /* Basis-function level description: exactly the reference's
@@ -216,7 +222,10 @@ typedef struct {
     int start_diis;             /* default 4 (scf.hpp:235) */
     int max_history;            /* default 8 (scf.hpp:236) */
     int verbose;
-    int reserved[6];
+    int eigensolver;            /* HFX_EIG_AUTO (0): density of each iteration by the SP2 projector on the device for
+                                   K <= 640, cuSOLVER syevd where it does not converge (no HOMO-LUMO gap) and once at
+                                   the end for the MO energies and coefficients; HFX_EIG_SYEVD: syevd every iteration */
+    int reserved[5];
 } hfx_scf_options;
 
 typedef struct {
@@ -231,7 +240,9 @@ typedef struct {
     int mixed_builds;           /* builds with FP32 quartets (mixed precision) */
     int fp64_builds;            /* full FP64 builds */
     int delta_builds;           /* FP64 builds of a density change (mixed precision, final cycles) */
-    int reserved[4];
+    int projections;            /* iterations whose density came from the SP2 projector (device SCF) */
+    int projection_fallbacks;   /* iterations where it did not converge and syevd was used */
+    int reserved[2];
 } hfx_scf_result;
 
 /* RHF (scf.hpp:205-419).  P0: optional K*K initial density (NULL = zero).
