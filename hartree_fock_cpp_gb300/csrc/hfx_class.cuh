@@ -167,36 +167,28 @@ __device__ __forceinline__ void boys_all(T Tv, const T* __restrict__ tab, T (&F)
         }
     } else {
         if (Tv < (T)kBoysTMax) {
+            // the (L, k) row: F_{L+j}(T_k) / j!, j = 0..6, then exp(-T_k)
             const int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
             const T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
-            const T* f = tab + k * kBoysM + L;
-            T r;
-            if constexpr (sizeof(T) == 8) {
-                r = __ldg(f + 6) * (T)(1.0 / 720.0);
-                r = fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
-                r = fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
-            } else {
-                r = __ldg(f + 4) * (T)(1.0 / 24.0);
-            }
-            r = fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
-            r = fma(r, nd, __ldg(f + 2) * (T)0.5);
-            r = fma(r, nd, __ldg(f + 1));
-            F[L] = fma(r, nd, __ldg(f));
+            const double2* row = reinterpret_cast<const double2*>(tab + ((size_t)L * kBoysN + k) * kBoys64Row);
+            const double2 c0 = __ldg(row), c1 = __ldg(row + 1), c2 = __ldg(row + 2), c3 = __ldg(row + 3);
+            T r = c3.x;
+            r = fma(r, nd, c2.y);
+            r = fma(r, nd, c2.x);
+            r = fma(r, nd, c1.y);
+            r = fma(r, nd, c1.x);
+            r = fma(r, nd, c0.y);
+            F[L] = fma(r, nd, c0.x);
             if constexpr (L > 0) {
-                T x;
-                if constexpr (sizeof(T) == 8) {
-                    x = (T)(1.0 / 5040.0);
-                    x = fma(x, nd, (T)(1.0 / 720.0));
-                    x = fma(x, nd, (T)(1.0 / 120.0));
-                    x = fma(x, nd, (T)(1.0 / 24.0));
-                } else {
-                    x = (T)(1.0 / 24.0);
-                }
+                T x = (T)(1.0 / 5040.0);
+                x = fma(x, nd, (T)(1.0 / 720.0));
+                x = fma(x, nd, (T)(1.0 / 120.0));
+                x = fma(x, nd, (T)(1.0 / 24.0));
                 x = fma(x, nd, (T)(1.0 / 6.0));
                 x = fma(x, nd, (T)0.5);
                 x = fma(x, nd, (T)1);
                 x = fma(x, nd, (T)1);
-                const T e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+                const T e = c3.y * x;
                 const T t2 = Tv + Tv;
     #pragma unroll
                 for (int m = L - 1; m >= 0; --m) F[m] = fma(t2, F[m + 1], e) * ((T)1 / (T)(2 * m + 1));

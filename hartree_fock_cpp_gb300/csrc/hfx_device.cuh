@@ -37,6 +37,12 @@ constexpr int kBoysN = kBoysTMax * kBoysInvStep + 1;
 // so that one evaluation is two 16-byte loads.
 constexpr int kBoys32MaxL = 12;
 constexpr int kBoys32Row = 8;
+// The FP64 Fock kernels' table, one 8-double row per (L, k): {F_L, F_{L+1},
+// F_{L+2}/2!, ..., F_{L+6}/6!, exp(-T_k)} at T_k = k/16, L <= kBoys64MaxL:
+// the 7-term Taylor expansion of F_L about T_k with its coefficients
+// pre-scaled (four 16-byte loads and six FMAs, no multiplies).
+constexpr int kBoys64MaxL = 12;
+constexpr int kBoys64Row = 8;
 
 // Primitive-pair geometry: p = alpha + beta and the product centre P.
 struct __align__(32) PairGeo {
@@ -192,7 +198,7 @@ struct WarpArgs {
     const Task* tasks;
     int ntasks;
     int* counter;
-    const T* boys;             // [kBoysN][kBoysM], column kBoysM-1 = exp(-T_k)
+    const T* boys;             // per-L rows: kBoys64Row doubles (FP64) / kBoys32Row floats (FP32)
     double thr;
     const double* Qbf;
     int K;

@@ -16,6 +16,11 @@
 #include "hfx_engine.hpp"
 
 #include <algorithm>
+#include <thread>
+#include <exception>
+#include <atomic>
+#include <cstdio>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -202,6 +207,7 @@ void Job::init(const hfx_options& opt)
     const std::vector<double>& tab = boys_table_host();
     d_boys_.upload(tab, stream_);
     d_boys32_.upload(boys_table32_host(), stream_);
+    d_boys64_.upload(boys_table64_host(), stream_);
     for (int s = 0; s < 3; ++s) {
         cudaStream_t st;
         cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -212,8 +218,17 @@ void Job::init(const hfx_options& opt)
     }
     cuda_check(cudaEventCreateWithFlags(&fork_ev_, cudaEventDisableTiming), "event");
 
+    // HFX_TRACE_SETUP: phase times of job creation on stderr
+    const bool trace = std::getenv("HFX_TRACE_SETUP") != nullptr;
+    auto tnow = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+        return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    auto t0 = tnow();
     build_pairs();
+    auto t1 = tnow();
     compute_schwarz();
+    auto t2 = tnow();
     {
         std::vector<float> q32(qbf_.begin(), qbf_.end());
         d_qbf32_.upload(q32, stream_);
@@ -237,7 +252,9 @@ void Job::init(const hfx_options& opt)
             d_active_.upload(on, stream_);
         }
     }
+    auto t3 = tnow();
     build_jk_groups(false, gs_fp64_);
+    auto t4 = tnow();
     if (mixed()) {
         build_jk_groups(true, gs_mixed_);
         // float density copies of the FP32 groups, allocated with the job so
@@ -246,6 +263,10 @@ void Job::init(const hfx_options& opt)
     }
     d_counters_.alloc(std::max<size_t>(1, std::max(gs_fp64_.groups.size(), gs_mixed_.groups.size())));
     cuda_check(cudaStreamSynchronize(stream_), "job setup");
+    if (trace)
+        std::fprintf(stderr, "job setup (K=%d): pairs %.1f ms, Schwarz %.1f ms, pair upload %.1f ms, FP64 plan %.1f ms, "
+                             "rest %.1f ms\n",
+                     basis_.K, ms(t0, t1), ms(t1, t2), ms(t2, t3), ms(t3, t4), ms(t4, tnow()));
 }
 
 Job::~Job()
@@ -276,6 +297,28 @@ const std::vector<double>& boys_table_host()
         return t;
     }();
     return tab;
+}
+
+const std::vector<double>& boys_table64_host()
+{
+    static const std::vector<double> t64 = [] {
+        const std::vector<double>& t = boys_table_host();
+        std::vector<double> v((size_t)(kBoys64MaxL + 1) * kBoysN * kBoys64Row, 0.0);
+        double fac = 1.0;
+        double inv_fact[7];
+        for (int j = 0; j < 7; ++j) {
+            inv_fact[j] = 1.0 / fac;
+            fac *= (double)(j + 1);
+        }
+        for (int L = 0; L <= kBoys64MaxL; ++L)
+            for (int k = 0; k < kBoysN; ++k) {
+                double* r = &v[((size_t)L * kBoysN + k) * kBoys64Row];
+                for (int j = 0; j < 7; ++j) r[j] = t[(size_t)k * kBoysM + L + j] * inv_fact[j];
+                r[7] = t[(size_t)k * kBoysM + (kBoysM - 1)];
+            }
+        return v;
+    }();
+    return t64;
 }
 
 const std::vector<float>& boys_table32_host()
@@ -319,8 +362,12 @@ static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost,
     std::vector<unsigned short> bin(n);
     std::vector<size_t> count(kBins + 1, 0);
     for (size_t i = 0; i < n; ++i) {
+        // 16 bins per octave: the exponent and the top four mantissa bits
+        // (monotonic in the cost, which is all the order needs)
         const double c = cost[i] > 1.0 ? cost[i] : 1.0;
-        int b = (int)(16.0 * std::log2(c));
+        unsigned long long bits;
+        std::memcpy(&bits, &c, sizeof(bits));
+        int b = (int)(((bits >> 52) - 1023) * 16 + ((bits >> 48) & 15));
         b = b < 0 ? 0 : (b >= kBins ? kBins - 1 : b);
         bin[i] = (unsigned short)(kBins - 1 - b);   // descending cost = ascending bin
         ++count[bin[i] + 1];
@@ -598,7 +645,7 @@ void Job::compute_schwarz()
         a.tasks = dts[ti].p;
         a.ntasks = (int)kv.second.size();
         a.counter = ctr.p + ti;
-        a.boys = d_boys_.p;
+        a.boys = d_boys64_.p;
         a.thr = -1.0;
         a.K = basis_.K;
         a.slice = slice;
@@ -690,32 +737,120 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     tasks.swap(sorted);
 }
 
+namespace {
+// f(i) for i in [0, n) on up to 16 host threads, indices handed out one at a
+// time; the first exception is rethrown after every thread has joined.
+template <typename F>
+void parallel_for(int n, F&& f)
+{
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nt = std::min(std::min(n, hw), 16);
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::exception_ptr err;
+    std::mutex emu;
+    auto work = [&] {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) return;
+            try {
+                f(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(emu);
+                if (!err) err = std::current_exception();
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    if (err) std::rethrow_exception(err);
+}
+}  // namespace
+
 void Job::build_jk_groups(bool mixed, GroupSet& gs)
 {
     clear_graphs();   // graphs hold the previous plan's task pointers
     const double thr = opt_.screening_threshold;
     const double tau = opt_.fp32_threshold;
-    auto pcof = [&](int p) { return pair_class(hpairs_[p].l0, hpairs_[p].l1); };
-    // buckets: small classes per (pcb, pck, fp32); warp classes per (fp32)
-    struct Bucket {
-        std::vector<std::pair<int, int>> q;   // surviving quartets (bra, ket)
-        double prims = 0.0;                   // their primitive quartets
-        std::vector<Task> t;
-        std::vector<double> cost;
-        std::vector<unsigned short> shape;    // (bra, ket) primitive pairs of a task, 8 bits each
+    const int np = (int)hpairs_.size();
+    // per shell pair: its class; per class pair: kernel form and algorithmic
+    // flops per primitive quartet
+    std::vector<unsigned char> pcls(np);
+    for (int p = 0; p < np; ++p) pcls[p] = (unsigned char)pair_class(hpairs_[p].l0, hpairs_[p].l1);
+    constexpr int kPC = (kMaxL + 1) * (kMaxL + 2) / 2;
+    int pl0[kPC], pl1[kPC];
+    for (int l0 = 0; l0 <= kMaxL; ++l0)
+        for (int l1 = 0; l1 <= l0; ++l1) {
+            pl0[pair_class(l0, l1)] = l0;
+            pl1[pair_class(l0, l1)] = l1;
+        }
+    bool small_ok[2][kPC][kPC];
+    double fpp_tab[kPC][kPC];
+    for (int a = 0; a < kPC; ++a)
+        for (int b = 0; b < kPC; ++b) {
+            small_ok[0][a][b] = is_small_class(a, b, false);
+            small_ok[1][a][b] = is_small_class(a, b, true);
+            fpp_tab[a][b] = flops_per_prim(pl0[a], pl1[a], pl0[b], pl1[b]);
+        }
+    // buckets: small classes per (fp32, pcb, pck) at fp32 * 100 + pcb * 10 + pck;
+    // the warp kernel's per fp32 at kWarpBucket + fp32
+    constexpr int kWarpBucket = 200, kBuckets = 202;
+    // Work units of the enumeration: ranges of bra-side shell pairs X of one
+    // molecule.  Every unit lists its surviving quartets per bucket in the
+    // serial visiting order (X ascending, Y by decreasing Schwarz bound), so
+    // that the units concatenated in order give the same lists, and the same
+    // plan, on any number of threads.
+    struct Unit {
+        int frag, x0, x1;
+        std::vector<std::vector<std::pair<int, int>>> q;   // per bucket: (bra, ket)
+        std::vector<double> prims;                         // per bucket: primitive quartets
+        std::vector<std::vector<Task>> t;                  // per bucket: tiles
+        std::vector<std::vector<double>> cost;
+        std::vector<std::vector<unsigned short>> shape;   // (bra, ket) primitive pairs of a task, 8 bits each
     };
-    std::vector<Bucket> small(2 * 100), warp(2);
-    for_each_surviving_quartet(thr, [&](int X, int Y) {
-            const double bound = qsh_[X] * qsh_[Y];
-            int bra = X, ket = Y;
-            if (pcof(Y) > pcof(X)) std::swap(bra, ket);
-            const bool f32 = mixed && bound < tau;
-            const int pcb = pcof(bra), pck = pcof(ket);
-            const bool sm = is_small_class(pcb, pck, f32);
-            Bucket& bk = sm ? small[(f32 ? 100 : 0) + pcb * 10 + pck] : warp[f32 ? 1 : 0];
-            bk.q.push_back({bra, ket});
-            bk.prims += (double)hpairs_[bra].npp * hpairs_[ket].npp;
+    constexpr int kUnitPairs = 24;
+    std::vector<Unit> units;
+    std::vector<std::vector<int>> qorder(frags_.count());
+    for (int fr = 0; fr < frags_.count(); ++fr) {
+        const int p0 = frags_.pbase[fr], p1 = frags_.pbase[fr + 1];
+        std::vector<int>& order = qorder[fr];
+        order.resize(p1 - p0);
+        std::iota(order.begin(), order.end(), p0);
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return qsh_[a] > qsh_[b]; });
+        for (int x = p0; x < p1; x += kUnitPairs) units.push_back(Unit{fr, x, std::min(p1, x + kUnitPairs)});
+    }
+    const int nu = (int)units.size();
+    parallel_for(nu, [&](int u) {
+        Unit& un = units[u];
+        un.q.resize(kBuckets);
+        un.prims.assign(kBuckets, 0.0);
+        const std::vector<int>& order = qorder[un.frag];
+        for (int X = un.x0; X < un.x1; ++X) {
+            if (qsh_[X] <= 0.0) continue;
+            const double need = thr / qsh_[X];
+            for (int Y : order) {
+                if (qsh_[Y] < need) break;
+                if (Y > X) continue;
+                const double bound = qsh_[X] * qsh_[Y];
+                int bra = X, ket = Y;
+                if (pcls[Y] > pcls[X]) std::swap(bra, ket);
+                const int f32 = mixed && bound < tau ? 1 : 0;
+                const int pcb = pcls[bra], pck = pcls[ket];
+                const int b = small_ok[f32][pcb][pck] ? f32 * 100 + pcb * 10 + pck : kWarpBucket + f32;
+                un.q[b].push_back({bra, ket});
+                un.prims[b] += (double)hpairs_[bra].npp * hpairs_[ket].npp;
+            }
+        }
     });
+    std::vector<double> bprims(kBuckets, 0.0);
+    for (const Unit& un : units)
+        for (int b = 0; b < kBuckets; ++b) bprims[b] += un.prims[b];
     // Tiles of primitive quartets.  A thread task holds at most
     // shape_.small_chunk primitive quartets and a warp task at most
     // shape_.warp_chunk; a launch group with too few primitive quartets to
@@ -729,43 +864,83 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     constexpr double kThreadFill = 4.0 * 128;   // threads per SM the thread-kernel groups should offer
     constexpr double kWarpFill = 16.0;          // warps per SM for the warp-kernel groups
     constexpr long long kMinThreadTile = 8, kMinWarpTile = 64;
-    auto tile = [&](Bucket& bk, bool sm) {
+    std::vector<long long> chunk(kBuckets, 1);
+    for (int b = 0; b < kBuckets; ++b) {
+        const bool sm = b < kWarpBucket;
         const double fill = (sm ? kThreadFill : kWarpFill) * nsm_;
         const long long cap = sm ? shape_.small_chunk : shape_.warp_chunk;
         const long long lo = sm ? kMinThreadTile : kMinWarpTile;
-        const long long c = std::max<long long>(std::min<long long>(lo, cap),
-                                                std::min<long long>(cap, (long long)std::ceil(bk.prims / fill)));
-        bk.t.reserve(bk.q.size());
-        bk.cost.reserve(bk.q.size());
-        for (const auto& bq : bk.q) {
-            const HostPair& b = hpairs_[bq.first];
-            const HostPair& k = hpairs_[bq.second];
-            const double fpp = flops_per_prim(b.l0, b.l1, k.l0, k.l1);
-            const long long pq = (long long)b.npp * k.npp;
-            const long long n = std::max<long long>(1, (pq + c - 1) / c);
-            const int nb = (int)std::min<long long>(b.npp, n);
-            const int nk = sm ? (int)std::min<long long>(k.npp, (n + nb - 1) / nb) : 1;
-            for (int x = 0; x < nb; ++x) {
-                const int i0 = (int)((long long)b.npp * x / nb), i1 = (int)((long long)b.npp * (x + 1) / nb);
-                for (int y = 0; y < nk; ++y) {
-                    const int k0 = (int)((long long)k.npp * y / nk), k1 = (int)((long long)k.npp * (y + 1) / nk);
-                    bk.t.push_back(make_task(bq.first, bq.second, i0, i1, k0, k1));
-                    bk.cost.push_back((double)(i1 - i0) * (k1 - k0) * fpp);
-                    if (sm) bk.shape.push_back((unsigned short)(std::min(i1 - i0, 255) * 256 + std::min(k1 - k0, 255)));
+        chunk[b] = std::max<long long>(std::min<long long>(lo, cap),
+                                       std::min<long long>(cap, (long long)std::ceil(bprims[b] / fill)));
+    }
+    parallel_for(nu, [&](int u) {
+        Unit& un = units[u];
+        un.t.resize(kBuckets);
+        un.cost.resize(kBuckets);
+        un.shape.resize(kBuckets);
+        for (int bkt = 0; bkt < kBuckets; ++bkt) {
+            const bool sm = bkt < kWarpBucket;
+            const long long c = chunk[bkt];
+            for (const auto& bq : un.q[bkt]) {
+                const HostPair& b = hpairs_[bq.first];
+                const HostPair& k = hpairs_[bq.second];
+                const double fpp = fpp_tab[pcls[bq.first]][pcls[bq.second]];
+                const long long pq = (long long)b.npp * k.npp;
+                const long long n = std::max<long long>(1, (pq + c - 1) / c);
+                const int nb = (int)std::min<long long>(b.npp, n);
+                const int nk = sm ? (int)std::min<long long>(k.npp, (n + nb - 1) / nb) : 1;
+                for (int x = 0; x < nb; ++x) {
+                    const int i0 = (int)((long long)b.npp * x / nb), i1 = (int)((long long)b.npp * (x + 1) / nb);
+                    for (int y = 0; y < nk; ++y) {
+                        const int k0 = (int)((long long)k.npp * y / nk), k1 = (int)((long long)k.npp * (y + 1) / nk);
+                        un.t[bkt].push_back(make_task(bq.first, bq.second, i0, i1, k0, k1));
+                        un.cost[bkt].push_back((double)(i1 - i0) * (k1 - k0) * fpp);
+                        if (sm)
+                            un.shape[bkt].push_back(
+                                (unsigned short)(std::min(i1 - i0, 255) * 256 + std::min(k1 - k0, 255)));
+                    }
                 }
             }
+            std::vector<std::pair<int, int>>().swap(un.q[bkt]);
         }
-        std::vector<std::pair<int, int>>().swap(bk.q);
+    });
+    // per bucket: the units' tiles in unit order, then ordered by cost
+    struct Bucket {
+        std::vector<Task> t;
+        std::vector<double> cost;
+        std::vector<unsigned short> shape;
+        std::vector<size_t> order;
     };
-    for (auto& bk : small)
-        if (!bk.q.empty()) tile(bk, true);
-    for (auto& bk : warp)
-        if (!bk.q.empty()) tile(bk, false);
+    std::vector<Bucket> bk(kBuckets);
+    parallel_for(kBuckets, [&](int b) {
+        size_t n = 0;
+        for (const Unit& un : units) n += un.t[b].size();
+        if (n == 0) return;
+        Bucket& B = bk[b];
+        B.t.reserve(n);
+        B.cost.reserve(n);
+        if (b < kWarpBucket) B.shape.reserve(n);
+        for (Unit& un : units) {
+            B.t.insert(B.t.end(), un.t[b].begin(), un.t[b].end());
+            B.cost.insert(B.cost.end(), un.cost[b].begin(), un.cost[b].end());
+            B.shape.insert(B.shape.end(), un.shape[b].begin(), un.shape[b].end());
+            std::vector<Task>().swap(un.t[b]);
+            std::vector<double>().swap(un.cost[b]);
+            std::vector<unsigned short>().swap(un.shape[b]);
+        }
+        B.order = order_by_cost_desc(B.cost, B.shape.empty() ? nullptr : &B.shape);
+    });
+    std::vector<Bucket>& small = bk;
+    Bucket* warp = &bk[kWarpBucket];
     std::vector<Task> all;
+    {
+        size_t total = 0;
+        for (const Bucket& B : bk) total += B.t.size();
+        all.reserve(total);
+    }
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();
     gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
-    auto sorted = [](Bucket& bk) { return order_by_cost_desc(bk.cost, bk.shape.empty() ? nullptr : &bk.shape); };
     for (int f = 0; f < 2; ++f)
         for (int pcb = 0; pcb < 10; ++pcb)
             for (int pck = 0; pck <= pcb; ++pck) {
@@ -778,7 +953,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 g.fp32 = f == 1;
                 g.off = all.size();
                 g.n = bk.t.size();
-                for (size_t i : sorted(bk)) {
+                for (size_t i : bk.order) {
                     all.push_back(bk.t[i]);
                     g.flops += bk.cost[i];
                     g.prims += (double)(bk.t[i].i1 - bk.t[i].i0) * (bk.t[i].k1 - bk.t[i].k0);
@@ -790,9 +965,8 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         Bucket& bk = warp[f];
         if (bk.t.empty()) continue;
         // tier the warp tasks by the shared-memory slice they need
-        std::vector<size_t> idx = sorted(bk);
         std::map<int, std::vector<size_t>> tiers;
-        for (size_t i : idx) {
+        for (size_t i : bk.order) {
             const HostPair& b = hpairs_[bk.t[i].bra];
             const HostPair& k = hpairs_[bk.t[i].ket];
             // tier by slice size (powers of two), so that tasks with small
@@ -1004,7 +1178,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                 void* prm[] = {&a};
                 sk.kernel(lane, ks, prm);
             } else {
-                SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys_.p,
+                SmallArgs<double> a{d_pairs_.p, d_rec64_.p, tasks + g.off, (int)g.n, d_boys64_.p,
                                     opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, Dsh, dthr,
                                     active, nullptr, nullptr, nullptr};
                 cuda_check(small_spec_f64(g.pcb, g.pck, nk, (int)g.n, &ks), "small-class kernel");
@@ -1023,7 +1197,7 @@ void Job::launch_jk(OpSink& sk, int nk, const double* Dj, const double* Dk, cons
                 sk.kernel(0, ks, prm);
             } else {
                 WarpArgs<double> a{d_pairs_.p, d_rec64_.p, d_pct_.p, d_abs_.p, d_kh_.p, d_kl_.p,
-                                   tasks + g.off, (int)g.n, ctr + gi, d_boys_.p,
+                                   tasks + g.off, (int)g.n, ctr + gi, d_boys64_.p,
                                    opt_.screening_threshold, d_qbf_.p, K, Dj, Dk, Dk2, J, Kx, Kx2, g.slice,
                                    g.lane_min_npp,
                                    Dsh, dthr, nullptr, nullptr, active, nullptr, nullptr, nullptr};

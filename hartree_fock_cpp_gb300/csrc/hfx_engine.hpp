@@ -37,6 +37,8 @@ bool is_small_class(int pcb, int pck, bool fp32);
 const std::vector<double>& boys_table_host();
 // The FP32 kernels' Boys table: 8 floats per (L <= kBoys32MaxL, k), see hfx_device.cuh.
 const std::vector<float>& boys_table32_host();
+// The FP64 Fock kernels' Boys table: 8 doubles per (L <= kBoys64MaxL, k), see hfx_device.cuh.
+const std::vector<double>& boys_table64_host();
 
 void cuda_check(cudaError_t e, const char* what);
 
@@ -339,7 +341,8 @@ private:
     DevBuf<DPair> d_pairs_;
     DevBuf<PairGeo> d_ppgeo_;
     DevBuf<double> d_epool_;
-    DevBuf<double> d_boys_;
+    DevBuf<double> d_boys_;     // [kBoysN][kBoysM] (k_quartet_eri)
+    DevBuf<double> d_boys64_;   // per-L rows (FP64 Fock and Schwarz kernels)
     DevBuf<double> d_qbf_;
     DevBuf<float> d_qbf32_;         // float copy of d_qbf_ (the FP32 kernels' screen)
     DevBuf<unsigned long long> d_qsh_;

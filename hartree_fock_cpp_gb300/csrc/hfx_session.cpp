@@ -60,8 +60,7 @@ FockSession::FockSession(int device, int nspin, double screening_threshold)
     cuda_check(cudaEventCreate(&ev1_), "event");
     anchor64_.alloc(32);
     anchor32_.alloc(64);
-    const std::vector<double>& tab = boys_table_host();
-    boys64_.upload(tab, stream_);
+    boys64_.upload(boys_table64_host(), stream_);
     boys32_.upload(boys_table32_host(), stream_);
     const ClassTables& ct = class_tables();
     pct_.upload(ct.tab, stream_);

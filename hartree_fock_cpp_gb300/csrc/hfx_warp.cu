@@ -63,44 +63,34 @@ __device__ __forceinline__ void boys_top(T Tv, int L, const T* __restrict__ tab,
             FL = (T)0;
             e = (T)0;
         }
-        return;
-    }
-    if (Tv < (T)kBoysTMax) {
+    } else if (Tv < (T)kBoysTMax) {
+        // FP64 table: one 8-double row per (L, k), Taylor terms pre-scaled
         table = true;
         int k = (int)(Tv * (T)kBoysInvStep + (T)0.5);
         T nd = (T)k * ((T)1 / (T)kBoysInvStep) - Tv;
-        const T* f = tab + k * kBoysM + L;
-        T r;
-        if (sizeof(T) == 8) {
-            r = __ldg(f + 6) * (T)(1.0 / 720.0);
-            r = w_fma(r, nd, __ldg(f + 5) * (T)(1.0 / 120.0));
-            r = w_fma(r, nd, __ldg(f + 4) * (T)(1.0 / 24.0));
-        } else {
-            r = __ldg(f + 4) * (T)(1.0 / 24.0);
-        }
-        r = w_fma(r, nd, __ldg(f + 3) * (T)(1.0 / 6.0));
-        r = w_fma(r, nd, __ldg(f + 2) * (T)0.5);
-        r = w_fma(r, nd, __ldg(f + 1));
-        FL = w_fma(r, nd, __ldg(f));
+        const double2* row = reinterpret_cast<const double2*>(tab + ((size_t)L * kBoysN + k) * kBoys64Row);
+        const double2 c0 = __ldg(row), c1 = __ldg(row + 1), c2 = __ldg(row + 2), c3 = __ldg(row + 3);
+        T r = c3.x;
+        r = w_fma(r, nd, c2.y);
+        r = w_fma(r, nd, c2.x);
+        r = w_fma(r, nd, c1.y);
+        r = w_fma(r, nd, c1.x);
+        r = w_fma(r, nd, c0.y);
+        FL = w_fma(r, nd, c0.x);
         // exp(-T) = exp(-T_k) exp(nd), |nd| <= 1/32
-        T x;
-        if (sizeof(T) == 8) {
-            x = (T)(1.0 / 5040.0);
-            x = w_fma(x, nd, (T)(1.0 / 720.0));
-            x = w_fma(x, nd, (T)(1.0 / 120.0));
-            x = w_fma(x, nd, (T)(1.0 / 24.0));
-        } else {
-            x = (T)(1.0 / 24.0);
-        }
+        T x = (T)(1.0 / 5040.0);
+        x = w_fma(x, nd, (T)(1.0 / 720.0));
+        x = w_fma(x, nd, (T)(1.0 / 120.0));
+        x = w_fma(x, nd, (T)(1.0 / 24.0));
         x = w_fma(x, nd, (T)(1.0 / 6.0));
         x = w_fma(x, nd, (T)0.5);
         x = w_fma(x, nd, (T)1);
         x = w_fma(x, nd, (T)1);
-        e = __ldg(tab + k * kBoysM + (kBoysM - 1)) * x;
+        e = c3.y * x;
     } else {
         table = false;
         FL = (T)0;
-        e = (sizeof(T) == 8 && L >= 5) ? (T)exp(-(double)Tv) : (T)0;
+        e = L >= 5 ? (T)exp(-(double)Tv) : (T)0;
     }
 }
 
