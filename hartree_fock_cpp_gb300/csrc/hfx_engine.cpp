@@ -16,6 +16,7 @@
 #include "hfx_engine.hpp"
 
 #include <algorithm>
+#include <memory>
 #include <thread>
 #include <exception>
 #include <atomic>
@@ -826,6 +827,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         for (int x = p0; x < p1; x += kUnitPairs) units.push_back(Unit{fr, x, std::min(p1, x + kUnitPairs)});
     }
     const int nu = (int)units.size();
+    const auto tp0 = std::chrono::steady_clock::now();
     parallel_for(nu, [&](int u) {
         Unit& un = units[u];
         un.q.resize(kBuckets);
@@ -873,6 +875,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         chunk[b] = std::max<long long>(std::min<long long>(lo, cap),
                                        std::min<long long>(cap, (long long)std::ceil(bprims[b] / fill)));
     }
+    const auto tp1 = std::chrono::steady_clock::now();
     parallel_for(nu, [&](int u) {
         Unit& un = units[u];
         un.t.resize(kBuckets);
@@ -912,6 +915,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         std::vector<size_t> order;
     };
     std::vector<Bucket> bk(kBuckets);
+    const auto tp2 = std::chrono::steady_clock::now();
     parallel_for(kBuckets, [&](int b) {
         size_t n = 0;
         for (const Unit& un : units) n += un.t[b].size();
@@ -930,69 +934,60 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         }
         B.order = order_by_cost_desc(B.cost, B.shape.empty() ? nullptr : &B.shape);
     });
-    std::vector<Bucket>& small = bk;
-    Bucket* warp = &bk[kWarpBucket];
-    std::vector<Task> all;
-    {
-        size_t total = 0;
-        for (const Bucket& B : bk) total += B.t.size();
-        all.reserve(total);
-    }
+    const auto tp3 = std::chrono::steady_clock::now();
+    // Launch groups: one per small-class bucket, then the warp buckets split
+    // into tiers by the per-warp shared-memory slice their tasks need (powers
+    // of two, so that tasks with small slices are not held to the occupancy
+    // of the largest one).  Each group is a list of (bucket, index) in cost
+    // order; their tasks are copied into the final array by parallel chunks.
+    struct Span {
+        int bucket;
+        std::vector<size_t> idx;   // empty: the bucket's whole cost order
+    };
     std::vector<LaunchGroup>& groups = gs.groups;
     groups.clear();
-    gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
+    std::vector<Span> spans;
     for (int f = 0; f < 2; ++f)
         for (int pcb = 0; pcb < 10; ++pcb)
             for (int pck = 0; pck <= pcb; ++pck) {
-                Bucket& bk = small[f * 100 + pcb * 10 + pck];
-                if (bk.t.empty()) continue;
+                const int b = f * 100 + pcb * 10 + pck;
+                if (bk[b].t.empty()) continue;
                 LaunchGroup g{};
                 g.kind = 0;
                 g.pcb = pcb;
                 g.pck = pck;
                 g.fp32 = f == 1;
-                g.off = all.size();
-                g.n = bk.t.size();
-                for (size_t i : bk.order) {
-                    all.push_back(bk.t[i]);
-                    g.flops += bk.cost[i];
-                    g.prims += (double)(bk.t[i].i1 - bk.t[i].i0) * (bk.t[i].k1 - bk.t[i].k0);
-                }
+                g.n = bk[b].t.size();
                 groups.push_back(g);
+                spans.push_back(Span{b, {}});
             }
     const size_t elem[2] = {sizeof(double), sizeof(float)};
     for (int f = 0; f < 2; ++f) {
-        Bucket& bk = warp[f];
-        if (bk.t.empty()) continue;
-        // tier the warp tasks by the shared-memory slice they need
-        std::map<int, std::vector<size_t>> tiers;
-        for (size_t i : bk.order) {
-            const HostPair& b = hpairs_[bk.t[i].bra];
-            const HostPair& k = hpairs_[bk.t[i].ket];
-            // tier by slice size (powers of two), so that tasks with small
-            // slices are not held to the occupancy of the largest one
-            int sl = warp_slice_elems(b.l0, b.l1, k.l0, k.l1, bk.t[i].k1 - bk.t[i].k0, shape_.lane_min_npp);
+        const Bucket& B = bk[kWarpBucket + f];
+        if (B.t.empty()) continue;
+        const size_t n = B.t.size();
+        std::vector<int> sl(n);
+        parallel_for((int)((n + 65535) / 65536), [&](int c) {
+            for (size_t i = (size_t)c * 65536; i < std::min(n, (size_t)(c + 1) * 65536); ++i) {
+                const HostPair& hb = hpairs_[B.t[i].bra];
+                const HostPair& hk = hpairs_[B.t[i].ket];
+                sl[i] = warp_slice_elems(hb.l0, hb.l1, hk.l0, hk.l1, B.t[i].k1 - B.t[i].k0, shape_.lane_min_npp);
+            }
+        });
+        std::map<int, std::pair<std::vector<size_t>, int>> tiers;   // tier -> (indices in cost order, max slice)
+        for (size_t i : B.order) {
             int tier = 0;
-            while ((512 << tier) < sl) ++tier;
-            tiers[tier].push_back(i);
+            while ((512 << tier) < sl[i]) ++tier;
+            auto& tr = tiers[tier];
+            tr.first.push_back(i);
+            tr.second = std::max(tr.second, sl[i]);
         }
         for (auto& kv : tiers) {
             LaunchGroup g{};
             g.kind = 1;
             g.fp32 = f == 1;
-            g.off = all.size();
-            g.n = kv.second.size();
-            int slice = 0;
-            for (size_t i : kv.second) {
-                const HostPair& b = hpairs_[bk.t[i].bra];
-                const HostPair& k = hpairs_[bk.t[i].ket];
-                slice = std::max(slice, warp_slice_elems(b.l0, b.l1, k.l0, k.l1, bk.t[i].k1 - bk.t[i].k0,
-                                                         shape_.lane_min_npp));
-                all.push_back(bk.t[i]);
-                g.flops += bk.cost[i];
-                g.prims += (double)(bk.t[i].i1 - bk.t[i].i0) * (bk.t[i].k1 - bk.t[i].k0);
-            }
-            g.slice = (slice + 1) & ~1;
+            g.n = kv.second.first.size();
+            g.slice = (kv.second.second + 1) & ~1;
             g.lane_min_npp = shape_.lane_min_npp;
             g.warps_per_cta = (int)std::max<size_t>(
                 1, std::min<size_t>((size_t)shape_.warp_max_warps, (200 * 1024 - kWarpSmemHeader) / (g.slice * elem[f])));
@@ -1001,23 +996,74 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             long long need = ((long long)g.n + g.warps_per_cta - 1) / g.warps_per_cta;
             g.grid = (int)std::min<long long>(need, (long long)nsm_ * ctas_per_sm);
             groups.push_back(g);
+            spans.push_back(Span{kWarpBucket + f, std::move(kv.second.first)});
         }
+    }
+    size_t total = 0;
+    for (LaunchGroup& g : groups) {
+        g.off = total;
+        total += g.n;
+    }
+    // copy in chunks of up to 65536 tasks; per chunk the flops, primitive
+    // quartets and whole-quartet tiles, summed per group in chunk order
+    struct Chunk {
+        int group;
+        size_t r0, r1;   // range within the group
+        double flops = 0.0, prims = 0.0;
+        long long whole = 0;
+    };
+    std::vector<Chunk> chunks;
+    for (int gi = 0; gi < (int)groups.size(); ++gi)
+        for (size_t r = 0; r < groups[gi].n; r += 65536)
+            chunks.push_back(Chunk{gi, r, std::min(groups[gi].n, r + 65536)});
+    std::unique_ptr<Task[]> all(new Task[std::max<size_t>(1, total)]);
+    parallel_for((int)chunks.size(), [&](int c) {
+        Chunk& ch = chunks[c];
+        const Span& sp = spans[ch.group];
+        const Bucket& B = bk[sp.bucket];
+        Task* out = all.get() + groups[ch.group].off;
+        for (size_t r = ch.r0; r < ch.r1; ++r) {
+            const size_t i = sp.idx.empty() ? B.order[r] : sp.idx[r];
+            const Task& t = B.t[i];
+            out[r] = t;
+            ch.flops += B.cost[i];
+            ch.prims += (double)(t.i1 - t.i0) * (t.k1 - t.k0);
+            if (t.i0 == 0 && t.k0 == 0) ++ch.whole;
+        }
+    });
+    gs.flops64 = gs.flops32 = gs.prims = gs.quartets32 = 0.0;
+    gs.nquartets = 0;
+    for (const Chunk& ch : chunks) {
+        LaunchGroup& g = groups[ch.group];
+        g.flops += ch.flops;
+        g.prims += ch.prims;
+        gs.nquartets += (int)ch.whole;
+        if (g.fp32) gs.quartets32 += (double)ch.whole;
     }
     for (const auto& g : groups) {
-        if (g.fp32) {
+        if (g.fp32)
             gs.flops32 += g.flops;
-            for (size_t i = g.off; i < g.off + g.n; ++i)
-                if (all[i].i0 == 0 && all[i].k0 == 0) gs.quartets32 += 1.0;
-        } else {
+        else
             gs.flops64 += g.flops;
-        }
         gs.prims += g.prims;
     }
-    gs.ntasks = (int)all.size();
-    gs.nquartets = 0;
-    for (const auto& t : all)
-        if (t.i0 == 0 && t.k0 == 0) ++gs.nquartets;
-    gs.tasks.upload(all, stream_);
+    gs.ntasks = (int)total;
+    const auto tp4 = std::chrono::steady_clock::now();
+    gs.tasks.alloc(total);
+    if (total > 0)
+        cuda_check(cudaMemcpyAsync(gs.tasks.p, all.get(), total * sizeof(Task), cudaMemcpyHostToDevice, stream_),
+                   "plan upload");
+    // the host array is freed on return: the copy must have read it
+    cuda_check(cudaStreamSynchronize(stream_), "plan upload");
+    if (std::getenv("HFX_TRACE_SETUP")) {
+        auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+            return std::chrono::duration<double, std::milli>(b - a).count();
+        };
+        const auto tp5 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "plan (%s, %d tasks): enumerate %.1f ms, tile %.1f ms, order %.1f ms, assemble %.1f ms, "
+                             "upload %.1f ms\n", mixed ? "mixed" : "fp64", gs.ntasks, ms(tp0, tp1), ms(tp1, tp2),
+                     ms(tp2, tp3), ms(tp3, tp4), ms(tp4, tp5));
+    }
 }
 
 StreamSink::StreamSink(cudaStream_t main, const std::vector<cudaStream_t>& aux, cudaEvent_t fork_ev,

@@ -246,3 +246,16 @@ def test_launch_shape_autotuner_keeps_results(precision):
             fb.set_launch_shape(64, 1024, 2, lane)
             G2 = fb.repulsion_matrix(P)
             assert np.abs(G2 - G0).max() < (1e-11 if precision == 0 else 1e-6)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_plan_is_independent_of_host_threads(precision):
+    """The launch plan is enumerated and tiled on host threads, the ranges
+    concatenated in order: two jobs of the same molecule get the same launch
+    groups (classes, task counts, flops, primitive quartets, grids)."""
+    kw = dict(config=W.n_decane(), basis_set="6-31G*", precision=precision, fp32_threshold=0.1)
+    with H.FockBuilder(**kw) as a, H.FockBuilder(**kw) as b:
+        pa, pb = a.plan(), b.plan()
+    assert len(pa) == len(pb) > 0
+    for ga, gb in zip(pa, pb):
+        assert ga == gb
