@@ -559,23 +559,20 @@ __device__ __forceinline__ void small_quartet(const SmallArgs<T>& a, const Task&
     }
 }
 
-// Ket component-pair blocks of a class kernel: float classes whose
-// accumulators would not fit the register file split their ket component
-// pairs over small_ncb(...) threads per task (each computes R, its block's
-// ket sums, its block's integrals and their digestion; J and K are linear in
-// the integrals), at most ~40 accumulators per thread.
+// Ket component-pair blocks of a class kernel: classes whose accumulators
+// would not fit the register file split their ket component pairs over
+// small_ncb(...) threads per task (each computes R, its block's ket sums,
+// its block's integrals and their digestion; J and K are linear in the
+// integrals), at most 36 (FP64) / 40 (FP32) accumulators per thread.
 template <typename T, int LA, int LB, int LC, int LD>
 __host__ __device__ constexpr int small_ncb()
 {
     constexpr int ncd = c_nc(LC) * c_nc(LD);
-    if constexpr (sizeof(T) == 8) {
-        return 1;
-    } else {
-        constexpr int nab = c_nc(LA) * c_nc(LB);
-        int nb = 1;
-        while (nb < ncd && nab * ((ncd + nb - 1) / nb) > 40) ++nb;
-        return nb;
-    }
+    constexpr int nab = c_nc(LA) * c_nc(LB);
+    constexpr int budget = sizeof(T) == 8 ? 36 : 40;   // accumulators per thread
+    int nb = 1;
+    while (nb < ncd && nab * ((ncd + nb - 1) / nb) > budget) ++nb;
+    return nb;
 }
 
 template <typename T, int LA, int LB, int LC, int LD, int NK>

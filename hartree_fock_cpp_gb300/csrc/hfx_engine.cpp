@@ -384,15 +384,13 @@ static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost,
 
 bool is_small_class(int pcb, int pck, bool fp32)
 {
-    static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0}};
-    // FP32 only: thread-per-quartet forms that fit the register file in float
-    static const int small32[][2] = {{2, 2}, {3, 2}, {4, 1}, {4, 2}, {4, 3}, {4, 4},
-                                     {5, 0}, {5, 1}, {5, 2}, {5, 3}};
+    // every class up to (dd|ds) with at most d functions; the larger ones
+    // split their ket component pairs over several threads per task
+    static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0},
+                                   {2, 2}, {3, 2}, {4, 1}, {4, 2}, {4, 3}, {4, 4}, {5, 0}, {5, 1}, {5, 2}, {5, 3}};
+    (void)fp32;
     for (auto& c : small)
         if (c[0] == pcb && c[1] == pck) return true;
-    if (fp32)
-        for (auto& c : small32)
-            if (c[0] == pcb && c[1] == pck) return true;
     return false;
 }
 

@@ -3,6 +3,8 @@
 
 namespace hfx {
 
+cudaError_t small_spec_f64x(int pcb, int pck, int nk, int ntasks, KernelSpec* s);   // hfx_small_f64x.cu
+
 // Pair class index pc = l0*(l0+1)/2 + l1; bra pc >= ket pc.  Returns
 // cudaErrorInvalidValue for a class that has no small-class kernel.
 cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
@@ -17,7 +19,7 @@ cudaError_t small_spec_f64(int pcb, int pck, int nk, int ntasks, KernelSpec* s)
     case 3 * 16 + 1: return small_spec<double, 2, 0, 1, 0>(nk, ntasks, s);   // (ds|ps)
     case 3 * 16 + 3: return small_spec<double, 2, 0, 2, 0>(nk, ntasks, s);   // (ds|ds)
     case 4 * 16 + 0: return small_spec<double, 2, 1, 0, 0>(nk, ntasks, s);   // (dp|ss)
-    default: return cudaErrorInvalidValue;
+    default: return small_spec_f64x(pcb, pck, nk, ntasks, s);
     }
 }
 

@@ -113,7 +113,11 @@ def test_request_arriving_mid_scf_joins_the_running_session():
     alone = [H.rhf_diis(j["config"], j["basis_set"], **kw) for j in jobs]
     with Server(max_active=4, pack_max=4, precision=H.HFX_PREC_MIXED, fp32_threshold=0.03) as srv:
         first = srv.submit(**jobs[0])
-        time.sleep(0.3)
+        # the second request arrives once the first is admitted (setting up or
+        # iterating: a whole n-decane SCF now takes well under a second)
+        t0 = time.time()
+        while srv.poll(first)["state"] == "queued" and time.time() - t0 < 60:
+            time.sleep(0.005)
         second = srv.submit(**jobs[1])
         srv.drain(600)
         infos = [srv.poll(first), srv.poll(second)]
