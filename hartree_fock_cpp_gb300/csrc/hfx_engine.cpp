@@ -382,6 +382,19 @@ static std::vector<size_t> order_by_cost_desc(const std::vector<double>& cost,
     return idx;
 }
 
+// The classes whose class kernels split their ket component pairs over
+// several threads per task (or, (dd|ss), hold 36 accumulators): in FP64 they
+// beat the warp kernel on lightly contracted quartets (benzene/cc-pVDZ build
+// 21.4 -> 17.9 ms) but not on heavily contracted ones (NaCl/cc-pVTZ 20.0 ->
+// 22.2 ms), whose quartets the plan keeps on the warp kernel.
+static bool is_ket_blocked_class(int pcb, int pck)
+{
+    static const int blocked[][2] = {{2, 2}, {3, 2}, {4, 1}, {4, 2}, {4, 3}, {4, 4}, {5, 0}, {5, 1}, {5, 2}, {5, 3}};
+    for (auto& c : blocked)
+        if (c[0] == pcb && c[1] == pck) return true;
+    return false;
+}
+
 bool is_small_class(int pcb, int pck, bool fp32)
 {
     // every class up to (dd|ds) with at most d functions; the larger ones
@@ -772,6 +785,10 @@ void parallel_for(int n, F&& f)
 }
 }  // namespace
 
+// FP64 quartets of the ket-blocked classes with more primitive quartets than
+// this run on the warp kernel.
+constexpr long long kKetBlockMaxPrims64 = 64;
+
 void Job::build_jk_groups(bool mixed, GroupSet& gs)
 {
     clear_graphs();   // graphs hold the previous plan's task pointers
@@ -790,11 +807,13 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             pl1[pair_class(l0, l1)] = l1;
         }
     bool small_ok[2][kPC][kPC];
+    bool ket_blocked[kPC][kPC];   // FP64 class kernels added beyond the nine single-block ones
     double fpp_tab[kPC][kPC];
     for (int a = 0; a < kPC; ++a)
         for (int b = 0; b < kPC; ++b) {
             small_ok[0][a][b] = is_small_class(a, b, false);
             small_ok[1][a][b] = is_small_class(a, b, true);
+            ket_blocked[a][b] = is_ket_blocked_class(a, b);
             fpp_tab[a][b] = flops_per_prim(pl0[a], pl1[a], pl0[b], pl1[b]);
         }
     // buckets: small classes per (fp32, pcb, pck) at fp32 * 100 + pcb * 10 + pck;
@@ -842,7 +861,13 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 if (pcls[Y] > pcls[X]) std::swap(bra, ket);
                 const int f32 = mixed && bound < tau ? 1 : 0;
                 const int pcb = pcls[bra], pck = pcls[ket];
-                const int b = small_ok[f32][pcb][pck] ? f32 * 100 + pcb * 10 + pck : kWarpBucket + f32;
+                // FP64 quartets of the ket-block classes with many primitive
+                // quartets go to the warp kernel: every ket block of a class
+                // kernel task recomputes R and the Boys function
+                const bool sm = small_ok[f32][pcb][pck] &&
+                                (f32 || !ket_blocked[pcb][pck] ||
+                                 (long long)hpairs_[bra].npp * hpairs_[ket].npp <= kKetBlockMaxPrims64);
+                const int b = sm ? f32 * 100 + pcb * 10 + pck : kWarpBucket + f32;
                 un.q[b].push_back({bra, ket});
                 un.prims[b] += (double)hpairs_[bra].npp * hpairs_[ket].npp;
             }
