@@ -1,9 +1,8 @@
-// hfx_small_f32x.cu -- float-only class kernels for the larger classes whose
-// thread-per-quartet form fits the register file in FP32 once their ket
-// component pairs are split over a few threads per task (in FP64 these
-// classes run on the warp kernel).  Split from hfx_small_f32.cu (and the d-d
-// classes into hfx_small_f32y/z/w.cu) so the translation units compile in
-// parallel.
+// hfx_small_f32x.cu -- float class kernels for the larger classes whose
+// thread-per-quartet form fits the register file once their ket component
+// pairs are split over a few threads per task (the double forms are in
+// hfx_small_f64x..v.cu).  Split from hfx_small_f32.cu (and the d-d classes
+// into hfx_small_f32y/z/w.cu) so the translation units compile in parallel.
 #include "hfx_class.cuh"
 
 namespace hfx {
