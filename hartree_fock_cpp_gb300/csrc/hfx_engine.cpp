@@ -448,34 +448,74 @@ const ClassTables& class_tables()
 // coefficient are left out (build_pair_data).
 constexpr double kPrimPairCut = 1e-18;
 
+namespace {
+// f(i) for i in [0, n) on up to 16 host threads, indices handed out one at a
+// time; the first exception is rethrown after every thread has joined.
+template <typename F>
+void parallel_for(int n, F&& f)
+{
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int nt = std::min(std::min(n, hw), 16);
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::exception_ptr err;
+    std::mutex emu;
+    auto work = [&] {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) return;
+            try {
+                f(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> lk(emu);
+                if (!err) err = std::current_exception();
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    if (err) std::rethrow_exception(err);
+}
+}  // namespace
+
 PairData build_pair_data(const Basis& basis, const Fragments& fr)
 {
     const ClassTables& ct = class_tables();
     const auto& sh = basis.shells;
-    PairData pd;
-    std::vector<double> Ex, Ey, Ez;
+    // the shell pairs in their final order; each is built on its own (host
+    // threads), then appended in that order, so the tables do not depend on
+    // the thread count
+    struct Item {
+        int f, A, B;
+    };
+    std::vector<Item> items;
     for (int f = 0; f < fr.count(); ++f)
-    for (int A = fr.sh[f]; A < fr.sh[f + 1]; ++A)
-        for (int B = fr.sh[f]; B <= A; ++B) {
-            int s0 = A, s1 = B;
-            if (sh[A].L < sh[B].L) std::swap(s0, s1);
+        for (int A = fr.sh[f]; A < fr.sh[f + 1]; ++A)
+            for (int B = fr.sh[f]; B <= A; ++B) items.push_back(Item{f, A, B});
+    struct PairOut {
+        std::vector<PairGeo> geo;
+        std::vector<double> epool, rec;
+    };
+    std::vector<PairOut> outs(items.size());
+    constexpr int kPairsPerUnit = 16;
+    parallel_for((int)((items.size() + kPairsPerUnit - 1) / kPairsPerUnit), [&](int u) {
+        std::vector<double> Ex, Ey, Ez;
+        const size_t i1 = std::min(items.size(), (size_t)(u + 1) * kPairsPerUnit);
+        for (size_t it = (size_t)u * kPairsPerUnit; it < i1; ++it) {
+            int s0 = items[it].A, s1 = items[it].B;
+            if (sh[s0].L < sh[s1].L) std::swap(s0, s1);
             const Shell& S0 = sh[s0];
             const Shell& S1 = sh[s1];
-            int l0 = S0.L, l1 = S1.L, L = l0 + l1;
-            int n0 = ncart(l0), n1 = ncart(l1), H = nherm(L);
-            HostPair hp;
-            hp.frag = f;
-            hp.s0 = s0;
-            hp.s1 = s1;
-            hp.l0 = l0;
-            hp.l1 = l1;
-            hp.same = (A == B);
-            hp.pp0 = (int)pd.geo.size();
-            hp.e_off = (long long)pd.epool.size();
-            const int pc = pair_class(l0, l1);
-            const PairClassTab& pt = ct.tab[pc];
-            const long long rec_off = (long long)pd.rec.size();
-            int nt = L + 1;
+            const int l0 = S0.L, l1 = S1.L, L = l0 + l1;
+            const int n0 = ncart(l0), n1 = ncart(l1), H = nherm(L);
+            const PairClassTab& pt = ct.tab[pair_class(l0, l1)];
+            const int nt = L + 1;
             // All primitive pairs of the shell pair first (geometry, dense E
             // block, record coefficients), then only those whose largest
             // Hermite->Cartesian coefficient reaches kPrimPairCut of the shell
@@ -483,88 +523,125 @@ PairData build_pair_data(const Basis& basis, const Fragments& fr)
             // exp(-mu |AB|^2) ~ 0) change no integral by more than ~1e-14 of
             // its size, and skipping them removes their primitive quartets
             // from every class kernel.
-            struct Prim {
-                double p, x, y, z, cmax;
-                std::vector<double> e, c;
-            };
-            std::vector<Prim> prims;
+            const int np = S0.nprim() * S1.nprim();
+            const size_t ne = (size_t)n0 * n1 * H;
+            std::vector<double> pgeo((size_t)np * 4), pe((size_t)np * ne, 0.0), pc((size_t)np * pt.ncoef), pmax(np, 0.0);
+            std::vector<int> pnc(np, 0);
             double cmax_pair = 0.0;
             for (int i = 0; i < S0.nprim(); ++i)
                 for (int j = 0; j < S1.nprim(); ++j) {
-                    double a = S0.exps[i], be = S1.exps[j], p = a + be;
+                    const int q = i * S1.nprim() + j;
+                    const double a = S0.exps[i], be = S1.exps[j], p = a + be;
                     hermite_1d(l0, l1, a, be, S0.x, S1.x, Ex);
                     hermite_1d(l0, l1, a, be, S0.y, S1.y, Ey);
                     hermite_1d(l0, l1, a, be, S0.z, S1.z, Ez);
-                    Prim pr;
-                    pr.p = p;
-                    pr.x = (a * S0.x + be * S1.x) / p;
-                    pr.y = (a * S0.y + be * S1.y) / p;
-                    pr.z = (a * S0.z + be * S1.z) / p;
-                    pr.cmax = 0.0;
-                    pr.e.assign((size_t)n0 * n1 * H, 0.0);
-                    pr.c.reserve((size_t)pt.ncoef);
+                    pgeo[4 * q] = p;
+                    pgeo[4 * q + 1] = (a * S0.x + be * S1.x) / p;
+                    pgeo[4 * q + 2] = (a * S0.y + be * S1.y) / p;
+                    pgeo[4 * q + 3] = (a * S0.z + be * S1.z) / p;
+                    double cmax = 0.0;
+                    int nc = 0;
+                    double* cq = pc.data() + (size_t)q * pt.ncoef;
                     for (int c0 = 0; c0 < n0; ++c0) {
                         int ax, ay, az;
                         component(l0, c0, ax, ay, az);
                         for (int c1 = 0; c1 < n1; ++c1) {
                             int bx, by, bz;
                             component(l1, c1, bx, by, bz);
-                            double w = S0.w[(size_t)c0 * S0.nprim() + i] * S1.w[(size_t)c1 * S1.nprim() + j];
-                            double* row = pr.e.data() + (size_t)(c0 * n1 + c1) * H;
+                            const double w = S0.w[(size_t)c0 * S0.nprim() + i] * S1.w[(size_t)c1 * S1.nprim() + j];
+                            double* row = pe.data() + (size_t)q * ne + (size_t)(c0 * n1 + c1) * H;
                             for (int t = 0; t <= ax + bx; ++t)
-                                for (int u = 0; u <= ay + by; ++u)
+                                for (int u2 = 0; u2 <= ay + by; ++u2)
                                     for (int v = 0; v <= az + bz; ++v) {
-                                        double c = w * Ex[((size_t)ax * (l1 + 1) + bx) * nt + t] *
-                                                   Ey[((size_t)ay * (l1 + 1) + by) * nt + u] *
-                                                   Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
-                                        row[herm_index(t, u, v)] = c;
-                                        pr.c.push_back(c);
-                                        pr.cmax = std::max(pr.cmax, std::fabs(c));
+                                        const double c = w * Ex[((size_t)ax * (l1 + 1) + bx) * nt + t] *
+                                                         Ey[((size_t)ay * (l1 + 1) + by) * nt + u2] *
+                                                         Ez[((size_t)az * (l1 + 1) + bz) * nt + v];
+                                        row[herm_index(t, u2, v)] = c;
+                                        cq[nc++] = c;
+                                        cmax = std::max(cmax, std::fabs(c));
                                     }
                         }
                     }
-                    cmax_pair = std::max(cmax_pair, pr.cmax);
-                    prims.push_back(std::move(pr));
+                    pnc[q] = nc;
+                    pmax[q] = cmax;
+                    cmax_pair = std::max(cmax_pair, cmax);
                 }
-            int npp = 0;
-            for (const Prim& pr : prims) {
-                if (pr.cmax < kPrimPairCut * cmax_pair) continue;
-                pd.geo.push_back(make_pairgeo(pr.p, pr.x, pr.y, pr.z));
-                pd.epool.insert(pd.epool.end(), pr.e.begin(), pr.e.end());
-                size_t rb = pd.rec.size();
-                pd.rec.resize(rb + pt.stride, 0.0);
-                pd.rec[rb] = pr.p;
-                pd.rec[rb + 1] = pr.x;
-                pd.rec[rb + 2] = pr.y;
-                pd.rec[rb + 3] = pr.z;
-                pd.rec[rb + 4] = 1.0 / pr.p;
-                for (size_t k = 0; k < pr.c.size(); ++k) pd.rec[rb + 5 + k] = pr.c[k];
-                ++npp;
+            PairOut& o = outs[it];
+            for (int q = 0; q < np; ++q) {
+                if (pmax[q] < kPrimPairCut * cmax_pair) continue;
+                o.geo.push_back(make_pairgeo(pgeo[4 * q], pgeo[4 * q + 1], pgeo[4 * q + 2], pgeo[4 * q + 3]));
+                o.epool.insert(o.epool.end(), pe.begin() + (size_t)q * ne, pe.begin() + (size_t)(q + 1) * ne);
+                const size_t rb = o.rec.size();
+                o.rec.resize(rb + pt.stride, 0.0);
+                o.rec[rb] = pgeo[4 * q];
+                o.rec[rb + 1] = pgeo[4 * q + 1];
+                o.rec[rb + 2] = pgeo[4 * q + 2];
+                o.rec[rb + 3] = pgeo[4 * q + 3];
+                o.rec[rb + 4] = 1.0 / pgeo[4 * q];
+                for (int k = 0; k < pnc[q]; ++k) o.rec[rb + 5 + k] = pc[(size_t)q * pt.ncoef + k];
             }
-            hp.npp = npp;
-            DPair d{};
-            d.bf0 = S0.bf0 - fr.bf[f];
-            d.bf1 = S1.bf0 - fr.bf[f];
-            d.l0 = l0;
-            d.l1 = l1;
-            d.pp0 = hp.pp0;
-            d.npp = npp;
-            d.e_off = hp.e_off;
-            d.same = hp.same ? 1 : 0;
-            d.id = (int)pd.hpairs.size();
-            d.qmax = 0.0;
-            d.rec_off = rec_off;
-            d.pc = pc;
-            d.sh0 = s0 - fr.sh[f];
-            d.sh1 = s1 - fr.sh[f];
-            d.kdim = fr.K(f);
-            d.pbase = fr.pbase[f];
-            d.frag = f;
-            d.moff = fr.moff[f];
-            d.qoff = fr.qoff[f];
-            pd.dpairs.push_back(d);
-            pd.hpairs.push_back(hp);
         }
+    });
+    PairData pd;
+    {
+        size_t ng = 0, nep = 0, nrec = 0;
+        for (const PairOut& o : outs) {
+            ng += o.geo.size();
+            nep += o.epool.size();
+            nrec += o.rec.size();
+        }
+        pd.geo.reserve(ng);
+        pd.epool.reserve(nep);
+        pd.rec.reserve(nrec);
+    }
+    for (size_t it = 0; it < items.size(); ++it) {
+        const int f = items[it].f, A = items[it].A, B = items[it].B;
+        int s0 = A, s1 = B;
+        if (sh[A].L < sh[B].L) std::swap(s0, s1);
+        const Shell& S0 = sh[s0];
+        const Shell& S1 = sh[s1];
+        const int l0 = S0.L, l1 = S1.L;
+        PairOut& o = outs[it];
+        HostPair hp{};
+        hp.frag = f;
+        hp.s0 = s0;
+        hp.s1 = s1;
+        hp.l0 = l0;
+        hp.l1 = l1;
+        hp.same = (A == B);
+        hp.pp0 = (int)pd.geo.size();
+        hp.e_off = (long long)pd.epool.size();
+        hp.npp = (int)o.geo.size();
+        const long long rec_off = (long long)pd.rec.size();
+        pd.geo.insert(pd.geo.end(), o.geo.begin(), o.geo.end());
+        pd.epool.insert(pd.epool.end(), o.epool.begin(), o.epool.end());
+        pd.rec.insert(pd.rec.end(), o.rec.begin(), o.rec.end());
+        PairOut().geo.swap(o.geo);
+        std::vector<double>().swap(o.epool);
+        std::vector<double>().swap(o.rec);
+        DPair d{};
+        d.bf0 = S0.bf0 - fr.bf[f];
+        d.bf1 = S1.bf0 - fr.bf[f];
+        d.l0 = l0;
+        d.l1 = l1;
+        d.pp0 = hp.pp0;
+        d.npp = hp.npp;
+        d.e_off = hp.e_off;
+        d.same = hp.same ? 1 : 0;
+        d.id = (int)pd.hpairs.size();
+        d.qmax = 0.0;
+        d.rec_off = rec_off;
+        d.pc = pair_class(l0, l1);
+        d.sh0 = s0 - fr.sh[f];
+        d.sh1 = s1 - fr.sh[f];
+        d.kdim = fr.K(f);
+        d.pbase = fr.pbase[f];
+        d.frag = f;
+        d.moff = fr.moff[f];
+        d.qoff = fr.qoff[f];
+        pd.dpairs.push_back(d);
+        pd.hpairs.push_back(hp);
+    }
     return pd;
 }
 
@@ -749,41 +826,6 @@ void Job::build_tasks(double thr, std::vector<Task>& tasks, int& maxacc, int& ma
     tasks.swap(sorted);
 }
 
-namespace {
-// f(i) for i in [0, n) on up to 16 host threads, indices handed out one at a
-// time; the first exception is rethrown after every thread has joined.
-template <typename F>
-void parallel_for(int n, F&& f)
-{
-    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int nt = std::min(std::min(n, hw), 16);
-    if (nt <= 1) {
-        for (int i = 0; i < n; ++i) f(i);
-        return;
-    }
-    std::atomic<int> next{0};
-    std::exception_ptr err;
-    std::mutex emu;
-    auto work = [&] {
-        for (;;) {
-            const int i = next.fetch_add(1);
-            if (i >= n) return;
-            try {
-                f(i);
-            } catch (...) {
-                std::lock_guard<std::mutex> lk(emu);
-                if (!err) err = std::current_exception();
-            }
-        }
-    };
-    std::vector<std::thread> pool;
-    pool.reserve(nt - 1);
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
-    work();
-    for (auto& th : pool) th.join();
-    if (err) std::rethrow_exception(err);
-}
-}  // namespace
 
 // FP64 quartets of the ket-blocked classes with more primitive quartets than
 // this run on the warp kernel.

@@ -79,12 +79,13 @@ static std::vector<double> fock_diis(const std::deque<std::vector<double>>& fh,
 // X = S^{-1/2} (linalg.hpp:132-147)
 static std::vector<double> xmatrix(int K, const std::vector<double>& S)
 {
-    std::vector<double> w(K), U(K * K), X(K * K, 0.0);
+    std::vector<double> w(K), U(K * K), X(K * K, 0.0), rs(K);
     sym_eig(K, S.data(), w.data(), U.data());
+    for (int k = 0; k < K; ++k) rs[k] = 1.0 / std::sqrt(w[k]);
     for (int i = 0; i < K; ++i)
         for (int j = 0; j < K; ++j) {
             double s = 0.0;
-            for (int k = 0; k < K; ++k) s += U[i * K + k] * (1.0 / std::sqrt(w[k])) * U[j * K + k];
+            for (int k = 0; k < K; ++k) s += U[i * K + k] * rs[k] * U[j * K + k];
             X[i * K + j] = s;
         }
     return X;
