@@ -307,3 +307,28 @@ def test_served_stream_properties():
             assert na == nb + 1 and na + nb == W.n_electrons(j["config"])
         else:
             assert W.n_electrons(j["config"]) % 2 == 0
+
+
+def test_pair_data_independent_of_host_threads():
+    """The pair records are built per shell pair on host threads and appended
+    in pair order: repeated builds give identical records, primitive-pair
+    geometry and E blocks (NaCl/cc-pVTZ: heavily contracted shells)."""
+    m = _lib.MoleculeArgs(W.nacl_scan(64)[20], "cc-pVTZ")
+
+    def build():
+        npp, nprim, nep = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _lib.check(_lib.lib.hfx_debug_pair_data(m.ref(), ctypes.byref(npp), ctypes.byref(nprim), ctypes.byref(nep),
+                                                None, None, None))
+        rec = np.zeros(10 * npp.value, dtype=np.int32)
+        geo = np.zeros(4 * nprim.value)
+        ep = np.zeros(nep.value)
+        _lib.check(_lib.lib.hfx_debug_pair_data(m.ref(), None, None, None, _lib.ptr(rec), _lib.ptr(geo), _lib.ptr(ep)))
+        return rec, geo, ep
+
+    first = build()
+    for _ in range(3):
+        again = build()
+        for a, b in zip(first, again):
+            assert a.shape == b.shape and np.array_equal(a, b)
+    rec = first[0].reshape(-1, 10)
+    assert np.all(np.diff(rec[:, 4]) == rec[:-1, 5])    # primitive-pair ranges back to back, in pair order
