@@ -395,13 +395,13 @@ static bool is_ket_blocked_class(int pcb, int pck)
     return false;
 }
 
-bool is_small_class(int pcb, int pck, bool fp32)
+bool is_small_class(int pcb, int pck)
 {
-    // every class up to (dd|ds) with at most d functions; the larger ones
-    // split their ket component pairs over several threads per task
+    // every class up to (dd|ds) with at most d functions, in both precisions;
+    // the larger ones split their ket component pairs over several threads
+    // per task
     static const int small[][2] = {{0, 0}, {1, 0}, {1, 1}, {2, 0}, {2, 1}, {3, 0}, {3, 1}, {3, 3}, {4, 0},
                                    {2, 2}, {3, 2}, {4, 1}, {4, 2}, {4, 3}, {4, 4}, {5, 0}, {5, 1}, {5, 2}, {5, 3}};
-    (void)fp32;
     for (auto& c : small)
         if (c[0] == pcb && c[1] == pck) return true;
     return false;
@@ -848,13 +848,12 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
             pl0[pair_class(l0, l1)] = l0;
             pl1[pair_class(l0, l1)] = l1;
         }
-    bool small_ok[2][kPC][kPC];
-    bool ket_blocked[kPC][kPC];   // FP64 class kernels added beyond the nine single-block ones
+    bool small_ok[kPC][kPC];
+    bool ket_blocked[kPC][kPC];   // the ten classes beyond the nine single-block ones
     double fpp_tab[kPC][kPC];
     for (int a = 0; a < kPC; ++a)
         for (int b = 0; b < kPC; ++b) {
-            small_ok[0][a][b] = is_small_class(a, b, false);
-            small_ok[1][a][b] = is_small_class(a, b, true);
+            small_ok[a][b] = is_small_class(a, b);
             ket_blocked[a][b] = is_ket_blocked_class(a, b);
             fpp_tab[a][b] = flops_per_prim(pl0[a], pl1[a], pl0[b], pl1[b]);
         }
@@ -906,7 +905,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
                 // FP64 quartets of the ket-block classes with many primitive
                 // quartets go to the warp kernel: every ket block of a class
                 // kernel task recomputes R and the Boys function
-                const bool sm = small_ok[f32][pcb][pck] &&
+                const bool sm = small_ok[pcb][pck] &&
                                 (f32 || !ket_blocked[pcb][pck] ||
                                  (long long)hpairs_[bra].npp * hpairs_[ket].npp <= kKetBlockMaxPrims64);
                 const int b = sm ? f32 * 100 + pcb * 10 + pck : kWarpBucket + f32;

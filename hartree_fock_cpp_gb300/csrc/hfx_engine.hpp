@@ -32,7 +32,7 @@ cudaError_t launch_warp(bool fp32, const void* args, int nk, int grid, int warps
 // ket npp >= lane_min_npp, 0: never) needs 32 R vectors, the level-parallel one a round
 int warp_slice_elems(int l0b, int l1b, int l0k, int l1k, int npp_ket, int lane_min_npp);
 constexpr int kDefaultLaneMinNpp = 6;
-bool is_small_class(int pcb, int pck, bool fp32);
+bool is_small_class(int pcb, int pck);
 // Boys table of the kernels ([kBoysN][kBoysM], last column exp(-T_k)), built once per process.
 const std::vector<double>& boys_table_host();
 // The FP32 kernels' Boys table: 8 floats per (L <= kBoys32MaxL, k), see hfx_device.cuh.
