@@ -18,9 +18,10 @@ namespace hfx {
 // takes about 2 log2(W / g) + 8 steps, each one symmetric n x n product; the
 // result equals C_occ C_occ^T of an exact eigensolve to rounding (~1e-14).
 //
-// Everything stays on the device (no host synchronisation): kMaxSteps launches
-// of the step kernel, each of which returns at once after convergence, then a
-// finishing kernel that copies the projector and writes a status word.
+// Everything stays on the device (no host synchronisation): a fixed number of
+// launches of the step kernel (at most kMaxSteps), each of which returns at
+// once after convergence, then a finishing kernel that copies the projector
+// and writes a status word.
 class Sp2Projector {
 public:
     static constexpr int kMaxN = 1024;       // shared-memory panels of the step kernel
