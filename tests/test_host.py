@@ -332,3 +332,26 @@ def test_pair_data_independent_of_host_threads():
             assert a.shape == b.shape and np.array_equal(a, b)
     rec = first[0].reshape(-1, 10)
     assert np.all(np.diff(rec[:, 4]) == rec[:-1, 5])    # primitive-pair ranges back to back, in pair order
+
+
+def test_sp2_control_gives_the_occupied_projector():
+    """The density step's control (tests/sp2_emulation.py, as hfx_sp2.cu runs
+    it): for Fock-like spectra with a gap the projector equals C_occ C_occ^T
+    of an eigendecomposition, within the 100-step cap; with a degenerate
+    HOMO/LUMO pair it reports no convergence (the SCF then uses syevd)."""
+    import sp2_emulation as S
+    rng = np.random.default_rng(7)
+    for n, nocc, gap in ((7, 2, 0.5), (40, 9, 0.3), (120, 21, 0.47), (160, 30, 0.05)):
+        lam = np.concatenate([rng.uniform(-20.0, -gap / 2, nocc), rng.uniform(gap / 2, 5.0, n - nocc)])
+        lam[nocc - 1], lam[nocc] = -gap / 2, gap / 2
+        Q, _ = np.linalg.qr(rng.normal(size=(n, n)))
+        F = (Q * lam) @ Q.T
+        D, steps = S.sp2_projector(F, nocc)
+        assert D is not None and 0 < steps <= 100, (n, steps)
+        w, V = np.linalg.eigh(F)
+        assert np.abs(D - V[:, :nocc] @ V[:, :nocc].T).max() < 1e-11
+    # degenerate level at the Fermi surface: three orbitals at 0 for one pair
+    lam = np.array([-2.0, -1.0, 0.0, 0.0, 0.0, 1.0, 2.0])
+    Q, _ = np.linalg.qr(rng.normal(size=(7, 7)))
+    D, steps = S.sp2_projector((Q * lam) @ Q.T, 3)
+    assert D is None and steps == 0
