@@ -866,7 +866,7 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
     // that the units concatenated in order give the same lists, and the same
     // plan, on any number of threads.
     struct Unit {
-        int frag, x0, x1;
+        int frag = 0, x0 = 0, x1 = 0;
         std::vector<std::vector<std::pair<int, int>>> q;   // per bucket: (bra, ket)
         std::vector<double> prims;                         // per bucket: primitive quartets
         std::vector<std::vector<Task>> t;                  // per bucket: tiles
@@ -882,7 +882,12 @@ void Job::build_jk_groups(bool mixed, GroupSet& gs)
         order.resize(p1 - p0);
         std::iota(order.begin(), order.end(), p0);
         std::sort(order.begin(), order.end(), [&](int a, int b) { return qsh_[a] > qsh_[b]; });
-        for (int x = p0; x < p1; x += kUnitPairs) units.push_back(Unit{fr, x, std::min(p1, x + kUnitPairs)});
+        for (int x = p0; x < p1; x += kUnitPairs) {
+            units.emplace_back();
+            units.back().frag = fr;
+            units.back().x0 = x;
+            units.back().x1 = std::min(p1, x + kUnitPairs);
+        }
     }
     const int nu = (int)units.size();
     const auto tp0 = std::chrono::steady_clock::now();
